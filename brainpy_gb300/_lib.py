@@ -1,0 +1,81 @@
+"""ctypes binding of libbpgpu.so.
+
+The library is the only compute path: if it is missing, importing an operator
+module raises immediately (there is no CPU or PyTorch fallback).
+"""
+import ctypes
+import os
+
+import torch
+
+from . import _build
+
+_LIB = None
+
+BP_OK, BP_EINVAL, BP_ESHAPE, BP_EDTYPE, BP_ENOMEM, BP_ETIMEOUT, BP_ECUDA, BP_ENOTSUP = range(8)
+BP_I32, BP_I64 = 0, 1
+BP_EV_BOOL, BP_EV_F32_POS, BP_EV_F32_NZ = 0, 1, 2
+
+_c_i64 = ctypes.c_int64
+_c_i32 = ctypes.c_int32
+_c_u32 = ctypes.c_uint32
+_c_f32 = ctypes.c_float
+_c_size = ctypes.c_size_t
+_c_ptr = ctypes.c_void_p
+
+# name -> (restype, argtypes); kept in the same order as include/bpgpu.h
+SIGNATURES = {
+    "bp_status_string": (ctypes.c_char_p, [_c_i32]),
+    "bp_last_error": (ctypes.c_char_p, []),
+    "bp_version": (_c_i32, []),
+    "bp_event_info_workspace_size": (_c_size, [_c_i64]),
+    "bp_event_info": (_c_i32, [_c_ptr, _c_i32, _c_i64, _c_ptr, _c_ptr, _c_ptr, _c_size, _c_ptr]),
+    "bp_event_csrmv_workspace_size": (_c_size, [_c_i64, _c_i64, _c_i32]),
+    "bp_event_csrmv": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_ptr, _c_i32, _c_i64, _c_i64,
+                                _c_i32, _c_ptr, _c_ptr, _c_size, _c_ptr]),
+}
+
+
+class BPError(RuntimeError):
+  pass
+
+
+def lib():
+  """Loads libbpgpu.so (raises if it has not been built)."""
+  global _LIB
+  if _LIB is None:
+    path = _build.LIB
+    if not os.path.exists(path):
+      raise ImportError(f"{path} is missing: build it first (python -c 'import __graft_entry__ as g; g.build()' "
+                        "or python -m brainpy_gb300._build); brainpy_gb300 has no fallback compute path")
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+      fn = getattr(L, name)
+      fn.restype = res
+      fn.argtypes = args
+    _LIB = L
+  return _LIB
+
+
+def check(status, what):
+  if status == BP_OK:
+    return
+  msg = lib().bp_last_error().decode(errors="replace")
+  full = f"{what}: {lib().bp_status_string(status).decode()}: {msg}"
+  if status in (BP_ESHAPE, BP_EINVAL):
+    raise ValueError(full)
+  if status == BP_EDTYPE:
+    raise TypeError(full)
+  raise BPError(full)
+
+
+def stream_handle(device=None):
+  return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def ptr(t):
+  return ctypes.c_void_p(t.data_ptr()) if t is not None and t.numel() > 0 else ctypes.c_void_p(0)
+
+
+def workspace(nbytes, device):
+  return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=device)

@@ -1,0 +1,374 @@
+// event_csrmv.cu -- event.info and event.csrmv on plain CSR.
+//
+// event.csrmv, transpose=1 (the event-driven form): the spike vector is compacted to
+// the list of active rows, then one warp per active row streams the row's column
+// indices and adds into the output.  Homogeneous weights accumulate exact uint32
+// event counts (out = count * w at the end); heterogeneous weights accumulate float32.
+// transpose=0: one warp per row gathers the event flags of its columns.
+//
+// Reference semantics: brainpy/_src/math/event/_csr_matvec.py:321-412 (Numba CPU),
+// brainpy/_src/math/event/_csr_matvec_taichi.py:158-312 (Taichi GPU: warp per row,
+// global atomics).
+#include "common.cuh"
+#include "compact.cuh"
+
+namespace bp {
+
+// ---------------------------------------------------------------------------
+// ordered compaction (event.info)
+// ---------------------------------------------------------------------------
+constexpr int kInfoThreads = 256;
+constexpr int kInfoChunk = kInfoThreads * 16;  // events per block
+
+template <int ET>
+__global__ void __launch_bounds__(kInfoThreads) info_count_kernel(const void* __restrict__ events, int64_t n,
+                                                                  int32_t* __restrict__ block_counts) {
+  const bool vec_ok = ((reinterpret_cast<uintptr_t>(events) & 15u) == 0);
+  int64_t base = (int64_t)blockIdx.x * kInfoChunk + (int64_t)threadIdx.x * 16;
+  uint32_t mask = base < n ? load_event_mask16<ET>(events, base, n, vec_ok) : 0u;
+  int c = __popc(mask);
+  __shared__ int warp_tot[kInfoThreads / 32];
+  c = warp_sum(c);
+  if (lane_id() == 0) warp_tot[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int s = 0;
+    for (int w = 0; w < kInfoThreads / 32; ++w) s += warp_tot[w];
+    block_counts[blockIdx.x] = s;
+  }
+}
+
+// Exclusive scan of block_counts in place (single block); total -> *num.
+__global__ void __launch_bounds__(1024) info_scan_kernel(int32_t* __restrict__ block_counts, int nb,
+                                                         int32_t* __restrict__ num) {
+  __shared__ int warp_tot[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += 1024) {
+    int i = base + threadIdx.x;
+    int v = i < nb ? block_counts[i] : 0;
+    int incl = v;
+    const int lane = lane_id(), w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_tot[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+      int t = warp_tot[lane];
+      int ti = t;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int u = __shfl_up_sync(0xffffffffu, ti, o);
+        if (lane >= o) ti += u;
+      }
+      warp_tot[lane] = ti - t;
+    }
+    __syncthreads();
+    int excl = carry + warp_tot[w] + incl - v;
+    if (i < nb) block_counts[i] = excl;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *num = carry;
+}
+
+template <int ET>
+__global__ void __launch_bounds__(kInfoThreads) info_write_kernel(const void* __restrict__ events, int64_t n,
+                                                                  const int32_t* __restrict__ block_offsets,
+                                                                  const int32_t* __restrict__ num,
+                                                                  int32_t* __restrict__ ids) {
+  const bool vec_ok = ((reinterpret_cast<uintptr_t>(events) & 15u) == 0);
+  const int64_t blk0 = (int64_t)blockIdx.x * kInfoChunk;
+  int64_t base = blk0 + (int64_t)threadIdx.x * 16;
+  uint32_t mask = base < n ? load_event_mask16<ET>(events, base, n, vec_ok) : 0u;
+  int c = __popc(mask);
+  const int lane = lane_id(), w = threadIdx.x >> 5;
+  int incl = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  __shared__ int warp_tot[kInfoThreads / 32];
+  if (lane == 31) warp_tot[w] = incl;
+  __syncthreads();
+  int wpre = 0;
+  for (int k = 0; k < w; ++k) wpre += warp_tot[k];
+  int pos = block_offsets[blockIdx.x] + wpre + incl - c;
+  while (mask) {
+    int k = __ffs(mask) - 1;
+    mask &= mask - 1;
+    ids[pos++] = (int32_t)(base + k);
+  }
+  // pad: output positions of this block's range that lie beyond the total count
+  const int total = *num;
+  for (int64_t p = blk0 + threadIdx.x; p < blk0 + kInfoChunk && p < n; p += kInfoThreads)
+    if (p >= total) ids[p] = -1;
+}
+
+// ---------------------------------------------------------------------------
+// event.csrmv kernels
+// ---------------------------------------------------------------------------
+template <typename IdxT>
+__device__ __forceinline__ void row_bounds(const IdxT* indptr, int64_t row, int64_t nnz, int64_t& b, int64_t& e) {
+  b = (int64_t)indptr[row];
+  e = (int64_t)indptr[row + 1];
+  b = b < 0 ? 0 : (b > nnz ? nnz : b);
+  e = e < b ? b : (e > nnz ? nnz : e);
+}
+
+// transpose=1, one warp per active row, global atomics.
+template <typename IdxT, bool HOMO>
+__global__ void __launch_bounds__(256) ecsr_t_rowpar_kernel(const IdxT* __restrict__ indptr,
+                                                            const IdxT* __restrict__ indices,
+                                                            const float* __restrict__ data, int64_t nnz,
+                                                            int64_t n, const int32_t* __restrict__ list,
+                                                            const int32_t* __restrict__ count, void* out) {
+  const int lane = lane_id();
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t a_total = *count;
+  for (int64_t a = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); a < a_total; a += nwarps) {
+    const int64_t row = list[a];
+    int64_t b, e;
+    row_bounds(indptr, row, nnz, b, e);
+    int64_t j = b + lane;
+    for (; j + 96 < e; j += 128) {
+      int64_t c0 = (int64_t)indices[j], c1 = (int64_t)indices[j + 32];
+      int64_t c2 = (int64_t)indices[j + 64], c3 = (int64_t)indices[j + 96];
+      if (HOMO) {
+        unsigned* o = static_cast<unsigned*>(out);
+        if ((uint64_t)c0 < (uint64_t)n) atomicAdd(o + c0, 1u);
+        if ((uint64_t)c1 < (uint64_t)n) atomicAdd(o + c1, 1u);
+        if ((uint64_t)c2 < (uint64_t)n) atomicAdd(o + c2, 1u);
+        if ((uint64_t)c3 < (uint64_t)n) atomicAdd(o + c3, 1u);
+      } else {
+        float w0 = data[j], w1 = data[j + 32], w2 = data[j + 64], w3 = data[j + 96];
+        float* o = static_cast<float*>(out);
+        if ((uint64_t)c0 < (uint64_t)n) atomicAdd(o + c0, w0);
+        if ((uint64_t)c1 < (uint64_t)n) atomicAdd(o + c1, w1);
+        if ((uint64_t)c2 < (uint64_t)n) atomicAdd(o + c2, w2);
+        if ((uint64_t)c3 < (uint64_t)n) atomicAdd(o + c3, w3);
+      }
+    }
+    for (; j < e; j += 32) {
+      int64_t c = (int64_t)indices[j];
+      if ((uint64_t)c < (uint64_t)n) {
+        if (HOMO) atomicAdd(static_cast<unsigned*>(out) + c, 1u);
+        else atomicAdd(static_cast<float*>(out) + c, data[j]);
+      }
+    }
+  }
+}
+
+// counts (uint32, in place) -> float32 count * w
+__global__ void counts_to_float_kernel(void* buf, int64_t n, const float* __restrict__ w_ptr) {
+  const float w = *w_ptr;
+  unsigned* u = static_cast<unsigned*>(buf);
+  float* f = static_cast<float*>(buf);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    f[i] = (float)u[i] * w;
+}
+
+template <int ET>
+__device__ __forceinline__ bool event_at(const void* events, int64_t i) {
+  if (ET == BP_EV_BOOL) return __ldg(static_cast<const uint8_t*>(events) + i) != 0;
+  return ev_on_f32(__ldg(static_cast<const float*>(events) + i), ET);
+}
+
+// transpose=0, one warp per row.
+template <typename IdxT, bool HOMO, int ET>
+__global__ void __launch_bounds__(256) ecsr_n_kernel(const IdxT* __restrict__ indptr,
+                                                     const IdxT* __restrict__ indices,
+                                                     const float* __restrict__ data, int64_t nnz, int64_t m,
+                                                     int64_t n, const void* __restrict__ events,
+                                                     float* __restrict__ out) {
+  const int lane = lane_id();
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < m; row += nwarps) {
+    int64_t b, e;
+    row_bounds(indptr, row, nnz, b, e);
+    unsigned cnt = 0;
+    float acc = 0.0f;
+    for (int64_t j = b + lane; j < e; j += 32) {
+      int64_t c = (int64_t)indices[j];
+      bool on = (uint64_t)c < (uint64_t)n && event_at<ET>(events, c);
+      if (HOMO) cnt += on;
+      else if (on) acc += data[j];
+    }
+    if (HOMO) {
+      cnt = warp_sum(cnt);
+      if (lane == 0) out[row] = (float)cnt * data[0];
+    } else {
+      acc = warp_sum(acc);
+      if (lane == 0) out[row] = acc;
+    }
+  }
+}
+
+static int grid_for(int64_t work_items, int per_block, int max_blocks) {
+  int64_t g = (work_items + per_block - 1) / per_block;
+  if (g < 1) g = 1;
+  if (g > max_blocks) g = max_blocks;
+  return (int)g;
+}
+
+template <int ET>
+static bp_status launch_compact(const void* events, int64_t m, int32_t* list, int32_t* count, cudaStream_t st) {
+  int grid = grid_for(m, 256 * 16, device_sm_count() * 8);
+  compact_unordered_kernel<ET><<<grid, 256, 0, st>>>(events, m, list, count);
+  return check_launch("compact_unordered_kernel");
+}
+
+bp_status compact_events(const void* events, bp_etype et, int64_t m, int32_t* list, int32_t* count,
+                         cudaStream_t st) {
+  switch (et) {
+    case BP_EV_BOOL: return launch_compact<BP_EV_BOOL>(events, m, list, count, st);
+    case BP_EV_F32_POS: return launch_compact<BP_EV_F32_POS>(events, m, list, count, st);
+    case BP_EV_F32_NZ: return launch_compact<BP_EV_F32_NZ>(events, m, list, count, st);
+  }
+  return BP_EINVAL;
+}
+
+template <typename IdxT>
+static bp_status ecsr_transpose_rowpar(const float* data, bool homo, const IdxT* indices, const IdxT* indptr,
+                                       int64_t nnz, const void* events, bp_etype et, int64_t m, int64_t n,
+                                       float* out, int32_t* list, int32_t* count, cudaStream_t st) {
+  BP_CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(int32_t), st));
+  BP_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * (size_t)n, st));
+  bp_status s = compact_events(events, et, m, list, count, st);
+  if (s != BP_OK) return s;
+  const int grid = device_sm_count() * 8;
+  if (homo) ecsr_t_rowpar_kernel<IdxT, true><<<grid, 256, 0, st>>>(indptr, indices, data, nnz, n, list, count, out);
+  else ecsr_t_rowpar_kernel<IdxT, false><<<grid, 256, 0, st>>>(indptr, indices, data, nnz, n, list, count, out);
+  if ((s = check_launch("ecsr_t_rowpar_kernel")) != BP_OK) return s;
+  if (homo) {
+    counts_to_float_kernel<<<grid_for(n, 256 * 4, device_sm_count() * 8), 256, 0, st>>>(out, n, data);
+    if ((s = check_launch("counts_to_float_kernel")) != BP_OK) return s;
+  }
+  return BP_OK;
+}
+
+template <typename IdxT, bool HOMO>
+static bp_status ecsr_n_dispatch(const float* data, const IdxT* indices, const IdxT* indptr, int64_t nnz,
+                                 const void* events, bp_etype et, int64_t m, int64_t n, float* out,
+                                 cudaStream_t st) {
+  const int grid = grid_for(m, 8, device_sm_count() * 16);
+  switch (et) {
+    case BP_EV_BOOL:
+      ecsr_n_kernel<IdxT, HOMO, BP_EV_BOOL><<<grid, 256, 0, st>>>(indptr, indices, data, nnz, m, n, events, out);
+      break;
+    case BP_EV_F32_POS:
+      ecsr_n_kernel<IdxT, HOMO, BP_EV_F32_POS><<<grid, 256, 0, st>>>(indptr, indices, data, nnz, m, n, events, out);
+      break;
+    case BP_EV_F32_NZ:
+      ecsr_n_kernel<IdxT, HOMO, BP_EV_F32_NZ><<<grid, 256, 0, st>>>(indptr, indices, data, nnz, m, n, events, out);
+      break;
+  }
+  return check_launch("ecsr_n_kernel");
+}
+
+}  // namespace bp
+
+using namespace bp;
+
+extern "C" {
+
+size_t bp_event_info_workspace_size(int64_t n) {
+  int64_t nb = (n + kInfoChunk - 1) / kInfoChunk;
+  return align_up(sizeof(int32_t) * (size_t)(nb > 0 ? nb : 1), 256);
+}
+
+bp_status bp_event_info(const void* events, bp_etype etype, int64_t n, int32_t* ids, int32_t* num_out,
+                        void* workspace, size_t workspace_bytes, bp_stream_t stream) {
+  clear_error();
+  cudaStream_t st = as_cuda(stream);
+  BP_REQUIRE(n >= 0, BP_EINVAL, "event_info: negative size %lld", (long long)n);
+  BP_REQUIRE(n <= INT32_MAX, BP_ENOTSUP, "event_info: n=%lld exceeds int32 ids", (long long)n);
+  BP_REQUIRE(etype >= BP_EV_BOOL && etype <= BP_EV_F32_NZ, BP_EINVAL, "event_info: bad etype %d", (int)etype);
+  BP_REQUIRE(num_out != nullptr, BP_EINVAL, "event_info: num_out is null");
+  if (n == 0) {
+    BP_CUDA_TRY(cudaMemsetAsync(num_out, 0, sizeof(int32_t), st));
+    return BP_OK;
+  }
+  BP_REQUIRE(events && ids, BP_EINVAL, "event_info: null events/ids");
+  BP_REQUIRE(workspace_bytes >= bp_event_info_workspace_size(n) && workspace, BP_ENOMEM,
+             "event_info: workspace %zu < %zu", workspace_bytes, bp_event_info_workspace_size(n));
+  int nb = (int)((n + kInfoChunk - 1) / kInfoChunk);
+  int32_t* bc = static_cast<int32_t*>(workspace);
+  switch (etype) {
+    case BP_EV_BOOL: info_count_kernel<BP_EV_BOOL><<<nb, kInfoThreads, 0, st>>>(events, n, bc); break;
+    case BP_EV_F32_POS: info_count_kernel<BP_EV_F32_POS><<<nb, kInfoThreads, 0, st>>>(events, n, bc); break;
+    case BP_EV_F32_NZ: info_count_kernel<BP_EV_F32_NZ><<<nb, kInfoThreads, 0, st>>>(events, n, bc); break;
+  }
+  bp_status s = check_launch("info_count_kernel");
+  if (s != BP_OK) return s;
+  info_scan_kernel<<<1, 1024, 0, st>>>(bc, nb, num_out);
+  if ((s = check_launch("info_scan_kernel")) != BP_OK) return s;
+  switch (etype) {
+    case BP_EV_BOOL: info_write_kernel<BP_EV_BOOL><<<nb, kInfoThreads, 0, st>>>(events, n, bc, num_out, ids); break;
+    case BP_EV_F32_POS: info_write_kernel<BP_EV_F32_POS><<<nb, kInfoThreads, 0, st>>>(events, n, bc, num_out, ids); break;
+    case BP_EV_F32_NZ: info_write_kernel<BP_EV_F32_NZ><<<nb, kInfoThreads, 0, st>>>(events, n, bc, num_out, ids); break;
+  }
+  return check_launch("info_write_kernel");
+}
+
+size_t bp_event_csrmv_workspace_size(int64_t m, int64_t n, int32_t transpose) {
+  (void)n;
+  if (!transpose) return 0;
+  return 256 + align_up(sizeof(int32_t) * (size_t)(m > 0 ? m : 1), 256);
+}
+
+bp_status bp_event_csrmv(const float* data, int64_t ndata, const void* indices, const void* indptr,
+                         bp_itype itype, int64_t nnz, const void* events, bp_etype etype, int64_t m,
+                         int64_t n, int32_t transpose, float* out, void* workspace,
+                         size_t workspace_bytes, bp_stream_t stream) {
+  clear_error();
+  cudaStream_t st = as_cuda(stream);
+  BP_REQUIRE(m >= 0 && n >= 0 && nnz >= 0, BP_EINVAL, "event_csrmv: negative size m=%lld n=%lld nnz=%lld",
+             (long long)m, (long long)n, (long long)nnz);
+  BP_REQUIRE(m <= INT32_MAX && n <= INT32_MAX, BP_ENOTSUP, "event_csrmv: dimensions beyond int32 range");
+  BP_REQUIRE(itype == BP_I32 || itype == BP_I64, BP_EDTYPE, "event_csrmv: bad index type %d", (int)itype);
+  BP_REQUIRE(etype >= BP_EV_BOOL && etype <= BP_EV_F32_NZ, BP_EDTYPE, "event_csrmv: bad event type %d", (int)etype);
+  BP_REQUIRE(ndata == 1 || ndata == nnz, BP_ESHAPE,
+             "event_csrmv: the size of data should be 1 or be consistent with indices (%lld vs %lld)",
+             (long long)ndata, (long long)nnz);
+  const int64_t n_out = transpose ? n : m;
+  if (n_out == 0) return BP_OK;
+  BP_REQUIRE(out != nullptr, BP_EINVAL, "event_csrmv: null out");
+  if (m == 0 || nnz == 0) {
+    BP_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * (size_t)n_out, st));
+    return BP_OK;
+  }
+  BP_REQUIRE(data && indices && indptr && events, BP_EINVAL, "event_csrmv: null data/indices/indptr/events");
+  const bool homo = ndata == 1;
+  if (transpose) {
+    BP_REQUIRE(workspace && workspace_bytes >= bp_event_csrmv_workspace_size(m, n, 1), BP_ENOMEM,
+               "event_csrmv: workspace %zu < %zu", workspace_bytes, bp_event_csrmv_workspace_size(m, n, 1));
+    int32_t* count = static_cast<int32_t*>(workspace);
+    int32_t* list = reinterpret_cast<int32_t*>(static_cast<char*>(workspace) + 256);
+    if (itype == BP_I32)
+      return ecsr_transpose_rowpar<int32_t>(data, homo, static_cast<const int32_t*>(indices),
+                                            static_cast<const int32_t*>(indptr), nnz, events, etype, m, n, out,
+                                            list, count, st);
+    return ecsr_transpose_rowpar<int64_t>(data, homo, static_cast<const int64_t*>(indices),
+                                          static_cast<const int64_t*>(indptr), nnz, events, etype, m, n, out, list,
+                                          count, st);
+  }
+  if (itype == BP_I32) {
+    auto ix = static_cast<const int32_t*>(indices);
+    auto ip = static_cast<const int32_t*>(indptr);
+    return homo ? ecsr_n_dispatch<int32_t, true>(data, ix, ip, nnz, events, etype, m, n, out, st)
+                : ecsr_n_dispatch<int32_t, false>(data, ix, ip, nnz, events, etype, m, n, out, st);
+  }
+  auto ix = static_cast<const int64_t*>(indices);
+  auto ip = static_cast<const int64_t*>(indptr);
+  return homo ? ecsr_n_dispatch<int64_t, true>(data, ix, ip, nnz, events, etype, m, n, out, st)
+              : ecsr_n_dispatch<int64_t, false>(data, ix, ip, nnz, events, etype, m, n, out, st);
+}
+
+}  // extern "C"

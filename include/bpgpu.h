@@ -1,0 +1,88 @@
+/*
+ * bpgpu.h -- C ABI of the GB300 (sm_103a) event-driven synaptic propagation
+ * library (libbpgpu.so).
+ *
+ * Conventions for every entry point:
+ *   - all array arguments are DEVICE pointers unless stated otherwise;
+ *   - work is enqueued on `stream`; no entry point synchronises the stream or
+ *     allocates device memory (scratch comes in through `workspace`);
+ *   - the return value is a bp_status; BP_OK means the work was enqueued;
+ *     bp_last_error() gives a message for the calling thread's last failure;
+ *   - outputs are fully overwritten (they need not be zeroed by the caller).
+ *
+ * The reference binds each operator as a legacy XLA custom call,
+ *   void target(cudaStream_t, void** buffers, const char* opaque, size_t len),
+ * with all validation done in Python before lowering.  The entry points below
+ * take the same operands as typed pointers plus the sizes that the reference
+ * packs into `opaque`, and validate them again on the host.
+ */
+#ifndef BPGPU_H_
+#define BPGPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* bp_stream_t; /* == cudaStream_t */
+
+typedef enum {
+  BP_OK = 0,
+  BP_EINVAL = 1,   /* bad argument (null pointer, negative size, bad flag) */
+  BP_ESHAPE = 2,   /* inconsistent shapes */
+  BP_EDTYPE = 3,   /* unsupported element type */
+  BP_ENOMEM = 4,   /* workspace / buffer too small */
+  BP_ETIMEOUT = 5, /* a bounded device-side wait gave up */
+  BP_ECUDA = 6,    /* CUDA runtime error */
+  BP_ENOTSUP = 7   /* valid request that this build does not implement */
+} bp_status;
+
+/* index type of CSR `indices` / `indptr` */
+typedef enum { BP_I32 = 0, BP_I64 = 1 } bp_itype;
+
+/* event vector type and the truth test applied to it:
+ *   BP_EV_BOOL     uint8 (bool) events, event = (e != 0)
+ *   BP_EV_F32_POS  float32 events, event = (e > 0)   -- Numba CPU kernels,
+ *                  brainpy/_src/math/event/_csr_matvec.py:343-361
+ *   BP_EV_F32_NZ   float32 events, event = (e != 0)  -- Taichi kernels,
+ *                  brainpy/_src/math/event/_csr_matvec_taichi.py:176-191 */
+typedef enum { BP_EV_BOOL = 0, BP_EV_F32_POS = 1, BP_EV_F32_NZ = 2 } bp_etype;
+
+const char* bp_status_string(bp_status s);
+const char* bp_last_error(void);
+/* library version, e.g. 0x000100 */
+int32_t bp_version(void);
+
+/* ---------------------------------------------------------------------------
+ * event.info -- spike compaction.
+ * Replaces the `event_info` custom call, brainpy/_src/math/event/_info_collection.py:24-43
+ * (Numba CPU kernel :144-155, brainpylib GPU target bound at :78-100).
+ * ids[0:num] = ascending indices i with event(events[i]); ids[num:n] = -1; num_out[0] = num.
+ * ------------------------------------------------------------------------- */
+size_t bp_event_info_workspace_size(int64_t n);
+bp_status bp_event_info(const void* events, bp_etype etype, int64_t n, int32_t* ids, int32_t* num_out,
+                        void* workspace, size_t workspace_bytes, bp_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * event.csrmv -- product of a CSR matrix (shape m x n) and an event vector.
+ * Replaces the custom-call family event_csrmv{_homo,_heter}_float{_int,_long}{_bool,}{_transpose,}
+ * bound at brainpy/_src/math/event/_csr_matvec.py:453-500 (Python front-end :38-110) and the
+ * Taichi twin csrmv_taichi, brainpy/_src/math/event/_csr_matvec_taichi.py:344-452.
+ *   transpose=1: out (n)  out[j] = sum_{i: event(events[i])} A[i, j]       (events length m)
+ *   transpose=0: out (m)  out[i] = sum_{j in row i, event(events[j])} A[i,j] (events length n)
+ * data: float32, ndata == 1 (homogeneous weight) or ndata == nnz (heterogeneous).
+ * Only the truth value of an event is used, never its magnitude (as in the reference).
+ * Homogeneous weight with any event type: exact integer event counts, out = (float)count * w.
+ * ------------------------------------------------------------------------- */
+size_t bp_event_csrmv_workspace_size(int64_t m, int64_t n, int32_t transpose);
+bp_status bp_event_csrmv(const float* data, int64_t ndata, const void* indices, const void* indptr,
+                         bp_itype itype, int64_t nnz, const void* events, bp_etype etype, int64_t m,
+                         int64_t n, int32_t transpose, float* out, void* workspace,
+                         size_t workspace_bytes, bp_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BPGPU_H_ */

@@ -11,6 +11,7 @@
 // global atomics).
 #include "common.cuh"
 #include "compact.cuh"
+#include "timer.cuh"
 
 namespace bp {
 
@@ -243,8 +244,11 @@ static bp_status ecsr_transpose_rowpar(const float* data, bool homo, const IdxT*
   bp_status s = compact_events(events, et, m, list, count, st);
   if (s != BP_OK) return s;
   const int grid = device_sm_count() * 8;
-  if (homo) ecsr_t_rowpar_kernel<IdxT, true><<<grid, 256, 0, st>>>(indptr, indices, data, nnz, n, list, count, out);
-  else ecsr_t_rowpar_kernel<IdxT, false><<<grid, 256, 0, st>>>(indptr, indices, data, nnz, n, list, count, out);
+  {
+    ScopedKernelTimer tk(st);
+    if (homo) ecsr_t_rowpar_kernel<IdxT, true><<<grid, 256, 0, st>>>(indptr, indices, data, nnz, n, list, count, out);
+    else ecsr_t_rowpar_kernel<IdxT, false><<<grid, 256, 0, st>>>(indptr, indices, data, nnz, n, list, count, out);
+  }
   if ((s = check_launch("ecsr_t_rowpar_kernel")) != BP_OK) return s;
   if (homo) {
     counts_to_float_kernel<<<grid_for(n, 256 * 4, device_sm_count() * 8), 256, 0, st>>>(out, n, data);
@@ -258,6 +262,7 @@ static bp_status ecsr_n_dispatch(const float* data, const IdxT* indices, const I
                                  const void* events, bp_etype et, int64_t m, int64_t n, float* out,
                                  cudaStream_t st) {
   const int grid = grid_for(m, 8, device_sm_count() * 16);
+  ScopedKernelTimer tk(st);
   switch (et) {
     case BP_EV_BOOL:
       ecsr_n_kernel<IdxT, HOMO, BP_EV_BOOL><<<grid, 256, 0, st>>>(indptr, indices, data, nnz, m, n, events, out);

@@ -82,6 +82,15 @@ bp_status bp_event_csrmv(const float* data, int64_t ndata, const void* indices, 
                          int64_t n, int32_t transpose, float* out, void* workspace,
                          size_t workspace_bytes, bp_stream_t stream);
 
+/* ---------------------------------------------------------------------------
+ * Kernel timing (benchmark support; no reference counterpart).
+ * When enabled, each operator's dominant kernel launch is bracketed by CUDA events on its
+ * stream; bp_timer_collect synchronises them and returns the summed time and launch count,
+ * then resets.  Disabled by default; enabling/disabling resets the record.
+ * ------------------------------------------------------------------------- */
+void bp_timer_enable(int32_t on);
+bp_status bp_timer_collect(double* total_ms, int64_t* launches);
+
 #ifdef __cplusplus
 }
 #endif

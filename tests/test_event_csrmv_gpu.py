@@ -1,0 +1,147 @@
+"""event.csrmv / event.info on the GPU against the oracle and the golden vectors.
+
+Bars: homogeneous weights -> bit-exact against the oracle's count form ((float)count*w);
+every case -> within 1e-5 of the FP64 sum, scaled by max(|y|, sum|terms|)."""
+import numpy as np
+import pytest
+import torch
+
+from golden_util import csr_keys, load, scaled_err
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def ev(bplib):
+  from brainpy_gb300.math import event
+  return event
+
+
+def _check(ev, orc, data, ind, ptr, events, shape, transpose, taichi=False):
+  dev = torch.device("cuda")
+  fn = ev.csrmv_taichi if taichi else ev.csrmv
+  d = torch.as_tensor(np.atleast_1d(data).astype(np.float32), device=dev)
+  y = fn(d, torch.as_tensor(ind, device=dev), torch.as_tensor(ptr, device=dev), torch.as_tensor(events, device=dev),
+         shape=shape, transpose=transpose).cpu().numpy()
+  r = orc.event_csrmv(data, ind, ptr, events, shape, transpose, ev_rule=orc.EV_F32_NZ if taichi else orc.EV_F32_POS)
+  assert y.dtype == np.float32 and y.shape == r["out64"].shape
+  assert scaled_err(y, r["out64"], r["abs64"]) < TOL
+  if r["count32"] is not None:
+    np.testing.assert_array_equal(y, r["count32"])
+  return y
+
+
+def test_golden_shapes(ev, orc):
+  cs = load("csr")
+  for key in csr_keys(cs):
+    shp, t = key.split("|")
+    m, n = (int(x) for x in shp.split("x"))
+    transpose = t == "T1"
+    ind, ptr = cs[key + "|indices"], cs[key + "|indptr"]
+    for wname in ("homo", "heter"):
+      if key + f"|event_bool_{wname}" not in cs.files:
+        continue
+      data = np.array([-0.7], np.float32) if wname == "homo" else cs[key + "|heter"]
+      for kind, events in (("event_bool", cs[key + "|events"]), ("event_float", cs[key + "|events_f"])):
+        y = _check(ev, orc, data, ind, ptr, events, (m, n), transpose)
+        # and against the reference's own outputs (golden), FP32 within tolerance
+        ref = cs[key + f"|{kind}_{wname}"]
+        r = orc.event_csrmv(data, ind, ptr, events, (m, n), transpose)
+        assert scaled_err(y, ref.astype(np.float64), r["abs64"]) < TOL
+
+
+@pytest.mark.parametrize("n,k", [(10000, 100), (10000, 1000), (100000, 100), (100000, 1000)])
+@pytest.mark.parametrize("rate", [0.005, 0.02, 0.1])
+def test_config_sweep_sizes(ev, orc, n, k, rate):
+  from brainpy_gb300.connect import bernoulli_events, fixed_prob_csr, normal_weights
+  ind, ptr = fixed_prob_csr(n, n, k, seed=0)
+  events = bernoulli_events(n, rate, seed=2).cpu().numpy()
+  ind_h, ptr_h = ind.cpu().numpy(), ptr.cpu().numpy()
+  _check(ev, orc, np.float32(1.0), ind_h, ptr_h, events, (n, n), True)
+  heter = normal_weights(ind.numel(), 0.5, 0.1, seed=1).cpu().numpy()
+  _check(ev, orc, heter, ind_h, ptr_h, events, (n, n), True)
+  if n <= 10000:
+    _check(ev, orc, np.float32(0.6), ind_h, ptr_h, events, (n, n), False)
+    _check(ev, orc, heter, ind_h, ptr_h, events, (n, n), False)
+
+
+def test_edge_cases(ev, orc):
+  rng = np.random.default_rng(5)
+  m, n = 300, 200
+  lens = rng.integers(0, 40, m)
+  lens[::7] = 0  # empty rows
+  ptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+  ind = np.concatenate([rng.permutation(n)[:l] for l in lens]).astype(np.int32)
+  heter = rng.normal(size=ind.size).astype(np.float32)
+  for events in (np.zeros(m, bool), np.ones(m, bool), rng.random(m) < 0.5):
+    for data in (np.float32(2.5), heter):
+      _check(ev, orc, data, ind, ptr, events, (m, n), True)
+  # int64 indices
+  _check(ev, orc, heter, ind.astype(np.int64), ptr.astype(np.int64), rng.random(m) < 0.3, (m, n), True)
+  # float events: negatives and zeros are not events under the `> 0` rule, are under `!= 0`
+  evf = rng.choice(np.array([0.0, 1.0, -1.0, 0.25], np.float32), m)
+  _check(ev, orc, heter, ind, ptr, evf, (m, n), True)
+  _check(ev, orc, heter, ind, ptr, evf, (m, n), True, taichi=True)
+  # unaligned event vector (a slice starting at an odd byte)
+  big = torch.as_tensor(rng.random(m + 1) < 0.4, device="cuda")
+  sl = big[1:]
+  y = ev.csrmv(1.0, torch.as_tensor(ind, device="cuda"), torch.as_tensor(ptr, device="cuda"), sl,
+               shape=(m, n), transpose=True).cpu().numpy()
+  r = orc.event_csrmv(np.float32(1.0), ind, ptr, sl.cpu().numpy(), (m, n), True)
+  np.testing.assert_array_equal(y, r["count32"])
+  # empty matrix
+  y = ev.csrmv(1.0, torch.zeros(0, dtype=torch.int32, device="cuda"), torch.zeros(5, dtype=torch.int32, device="cuda"),
+               torch.ones(4, dtype=torch.bool, device="cuda"), shape=(4, 9), transpose=True)
+  assert y.shape == (9,) and float(y.abs().sum()) == 0.0
+
+
+def test_shape_errors(ev):
+  ind = torch.zeros(4, dtype=torch.int32, device="cuda")
+  ptr = torch.tensor([0, 2, 4], dtype=torch.int32, device="cuda")
+  with pytest.raises(ValueError, match="Shape mismatch"):
+    ev.csrmv(1.0, ind, ptr, torch.ones(3, dtype=torch.bool, device="cuda"), shape=(2, 5), transpose=True)
+  with pytest.raises(ValueError, match="consistent with indices"):
+    ev.csrmv(torch.ones(3, device="cuda"), ind, ptr, torch.ones(2, dtype=torch.bool, device="cuda"), shape=(2, 5),
+             transpose=True)
+  with pytest.raises(ValueError, match="int32 or int64"):
+    ev.csrmv(1.0, ind.to(torch.int16), ptr, torch.ones(2, dtype=torch.bool, device="cuda"), shape=(2, 5),
+             transpose=True)
+
+
+def test_info(ev, orc):
+  cs = load("csr")
+  for n in (1, 5, 100, 1000, 4097):
+    e = cs[f"info|{n}|events"]
+    ids, num = ev.info(torch.as_tensor(e, device="cuda"))
+    np.testing.assert_array_equal(ids.cpu().numpy(), cs[f"info|{n}|ids"])
+    assert int(num.cpu()[0]) == int(cs[f"info|{n}|num"][0])
+  rng = np.random.default_rng(1)
+  for n in (4096 * 37 + 5, 10 ** 6):
+    e = rng.random(n) < 0.02
+    ids, num = ev.info(torch.as_tensor(e, device="cuda"))
+    rid, rnum = orc.event_info(e)
+    np.testing.assert_array_equal(ids.cpu().numpy(), rid)
+    assert int(num.cpu()[0]) == rnum
+
+
+def test_full_size_properties(ev):
+  """N = 1e6, fan-out 1000, 2 % events: size-independent identities.
+  (a) homo output / w is the exact integer count, summing to the number of events;
+  (b) linearity in the event set: disjoint halves add up exactly (integer counts)."""
+  from brainpy_gb300.connect import bernoulli_events, fixed_prob_csr
+  n, k = 10 ** 6, 1000
+  ind, ptr = fixed_prob_csr(n, n, k, seed=0)
+  events = bernoulli_events(n, 0.02, seed=2)
+  y = ev.csrmv(1.0, ind, ptr, events, shape=(n, n), transpose=True)
+  n_events = int(events.sum()) * k
+  assert float(y.double().sum()) == n_events
+  assert torch.equal(y, torch.round(y))
+  half = torch.zeros_like(events)
+  half[: n // 2] = events[: n // 2]
+  y1 = ev.csrmv(1.0, ind, ptr, half, shape=(n, n), transpose=True)
+  y2 = ev.csrmv(1.0, ind, ptr, events & ~half, shape=(n, n), transpose=True)
+  assert torch.equal(y1 + y2, y)
+  y3 = ev.csrmv(0.37, ind, ptr, events, shape=(n, n), transpose=True)
+  assert torch.equal(y3, y * np.float32(0.37))

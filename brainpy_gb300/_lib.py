@@ -33,6 +33,9 @@ SIGNATURES = {
     "bp_event_csrmv_workspace_size": (_c_size, [_c_i64, _c_i64, _c_i32]),
     "bp_event_csrmv": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_ptr, _c_i32, _c_i64, _c_i64,
                                 _c_i32, _c_ptr, _c_ptr, _c_size, _c_ptr]),
+    "bp_event_csrmv_noalloc_max_rows": (_c_i64, []),
+    "bp_event_csrmv_noalloc": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_ptr, _c_i32, _c_i64,
+                                        _c_i64, _c_i32, _c_ptr, _c_ptr]),
     "bp_timer_enable": (None, [_c_i32]),
     "bp_timer_collect": (_c_i32, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_c_i64)]),
 }

@@ -257,6 +257,21 @@ static bp_status ecsr_transpose_rowpar(const float* data, bool homo, const IdxT*
   return BP_OK;
 }
 
+// The transpose (event-driven) path on scratch supplied by the caller: `list` has room for
+// m int32 row ids and `count` is one int32 (both are reset here before use).
+bp_status event_csrmv_transpose_on_scratch(const float* data, bool homo, const void* indices, const void* indptr,
+                                           bp_itype itype, int64_t nnz, const void* events, bp_etype et,
+                                           int64_t m, int64_t n, float* out, int32_t* list, int32_t* count,
+                                           cudaStream_t st) {
+  if (itype == BP_I32)
+    return ecsr_transpose_rowpar<int32_t>(data, homo, static_cast<const int32_t*>(indices),
+                                          static_cast<const int32_t*>(indptr), nnz, events, et, m, n, out, list,
+                                          count, st);
+  return ecsr_transpose_rowpar<int64_t>(data, homo, static_cast<const int64_t*>(indices),
+                                        static_cast<const int64_t*>(indptr), nnz, events, et, m, n, out, list,
+                                        count, st);
+}
+
 template <typename IdxT, bool HOMO>
 static bp_status ecsr_n_dispatch(const float* data, const IdxT* indices, const IdxT* indptr, int64_t nnz,
                                  const void* events, bp_etype et, int64_t m, int64_t n, float* out,

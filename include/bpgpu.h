@@ -83,6 +83,23 @@ bp_status bp_event_csrmv(const float* data, int64_t ndata, const void* indices, 
                          size_t workspace_bytes, bp_stream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * event.csrmv with no allocation anywhere (no counterpart in the reference).
+ * For callers that can pass nothing but operands and the result buffer -- e.g. a legacy
+ * XLA custom-call target, which gets its buffers from XLA and has no scratch allocator,
+ * and must not cudaMalloc (that would synchronise the device mid-stream).  Same
+ * arguments and results as bp_event_csrmv minus the workspace.  The scratch of the
+ * transpose path is a fixed __device__ array inside the library, held by every GPU that
+ * loads it until exit, sized for at most bp_event_csrmv_noalloc_max_rows() rows (larger
+ * m with transpose=1 returns BP_ENOMEM).  All calls on a device share that array: calls
+ * whose GPU work overlaps race, so order them on one stream.  The first call on each
+ * device looks the array up (cudaGetSymbolAddress); make it before any stream capture.
+ * ------------------------------------------------------------------------- */
+int64_t bp_event_csrmv_noalloc_max_rows(void);
+bp_status bp_event_csrmv_noalloc(const float* data, int64_t ndata, const void* indices, const void* indptr,
+                                 bp_itype itype, int64_t nnz, const void* events, bp_etype etype, int64_t m,
+                                 int64_t n, int32_t transpose, float* out, bp_stream_t stream);
+
+/* ---------------------------------------------------------------------------
  * Kernel timing (benchmark support; no reference counterpart).
  * When enabled, each operator's dominant kernel launch is bracketed by CUDA events on its
  * stream; bp_timer_collect synchronises them and returns the summed time and launch count,

@@ -33,12 +33,25 @@ SIGNATURES = {
     "bp_event_csrmv_workspace_size": (_c_size, [_c_i64, _c_i64, _c_i32]),
     "bp_event_csrmv": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_ptr, _c_i32, _c_i64, _c_i64,
                                 _c_i32, _c_ptr, _c_ptr, _c_size, _c_ptr]),
+    "bp_csr_plan_default_tile": (_c_i32, [_c_i64, _c_i32]),
+    "bp_csr_plan_bytes": (_c_size, [_c_i64, _c_i64, _c_i64, _c_i32, _c_i32]),
+    "bp_csr_plan_build": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_i32, _c_ptr,
+                                   _c_size, _c_ptr, _c_ptr]),
+    "bp_event_csrmv_planned_workspace_size": (_c_size, [_c_ptr]),
+    "bp_event_csrmv_planned": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_i32, _c_ptr, _c_i32, _c_ptr, _c_size, _c_ptr]),
     "bp_event_csrmv_noalloc_max_rows": (_c_i64, []),
     "bp_event_csrmv_noalloc": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_ptr, _c_i32, _c_i64,
                                         _c_i64, _c_i32, _c_ptr, _c_ptr]),
     "bp_timer_enable": (None, [_c_i32]),
     "bp_timer_collect": (_c_i32, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_c_i64)]),
 }
+
+
+class CsrPlan(ctypes.Structure):
+  """Mirror of bp_csr_plan (include/bpgpu.h)."""
+  _fields_ = [("m", _c_i64), ("n", _c_i64), ("nnz", _c_i64), ("tile_w", _c_i32), ("n_tiles", _c_i32),
+              ("heter", _c_i32), ("reserved", _c_i32), ("entries", ctypes.c_uint64), ("mem", _c_ptr),
+              ("bytes", _c_size)]
 
 
 class BPError(RuntimeError):

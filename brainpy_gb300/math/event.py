@@ -5,14 +5,116 @@ brainpy/_src/math/event/_csr_matvec.py:38-110 (csrmv),
 brainpy/_src/math/event/_csr_matvec_taichi.py:344-452 (csrmv_taichi) and
 brainpy/_src/math/event/_info_collection.py:24-43 (info).
 """
-from typing import Tuple, Union
+import ctypes
+import os
+import weakref
+from typing import Optional, Tuple, Union
 
 import torch
 
 from .. import _lib
 from ._utils import as_tensor, default_device, event_type, float_data, index_type
 
-__all__ = ["csrmv", "csrmv_taichi", "info"]
+__all__ = ["csrmv", "csrmv_taichi", "info", "CSRPlan", "prepare"]
+
+
+class CSRPlan:
+  """Column-tiled layout of a CSR matrix for the event-driven (transpose) kernels.
+
+  Built once on the GPU from (indices, indptr[, heterogeneous data]); afterwards every
+  ``csrmv(..., transpose=True)`` on the same matrix streams tile-local uint16 indices and
+  accumulates in shared memory (see include/bpgpu.h, bp_csr_plan).  The plan holds its
+  own device memory; it is a function of the arrays at build time.
+  """
+
+  def __init__(self, indices, indptr, shape, data=None, tile_w=None, cluster=4):
+    dev = indices.device
+    self.shape = (int(shape[0]), int(shape[1]))
+    self.cluster = int(cluster)
+    m, n = self.shape
+    L = _lib.lib()
+    heter = data is not None and data.numel() > 1
+    if tile_w is None:
+      tile_w = L.bp_csr_plan_default_tile(n, self.cluster)
+      if tile_w <= 0:
+        raise _lib.BPError("bp_csr_plan_default_tile failed: " + L.bp_last_error().decode())
+    self.tile_w = int(tile_w)
+    nbytes = L.bp_csr_plan_bytes(m, n, indices.numel(), int(heter), self.tile_w)
+    self.mem = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=dev)
+    self.c = _lib.CsrPlan()
+    itype = index_type(indices, "indices")
+    st = L.bp_csr_plan_build(_lib.ptr(data) if heter else None, data.numel() if heter else 1, _lib.ptr(indices),
+                             _lib.ptr(indptr), itype, indices.numel(), m, n, self.tile_w, _lib.ptr(self.mem),
+                             nbytes, ctypes.byref(self.c), _lib.stream_handle(dev))
+    _lib.check(st, "csr_plan_build")
+    self.heter = bool(heter)
+    self.device = dev
+
+  def csrmv(self, events, data=None, out=None, float_rule=_lib.BP_EV_F32_POS):
+    """out (n) = event-driven transpose product on this plan."""
+    dev = self.device
+    etype, ev = event_type(events, float_rule)
+    m, n = self.shape
+    if ev.shape[0] != m:
+      raise ValueError(f"Shape mismatch, vec ({ev.shape[0]},) @ mat {self.shape}.")
+    if out is None:
+      out = torch.empty(n, dtype=torch.float32, device=dev)
+    L = _lib.lib()
+    w = None
+    if not self.heter:
+      w = data if data is not None else torch.ones(1, dtype=torch.float32, device=dev)
+    ws_bytes = L.bp_event_csrmv_planned_workspace_size(ctypes.byref(self.c))
+    ws = _lib.workspace(ws_bytes, dev)
+    st = L.bp_event_csrmv_planned(ctypes.byref(self.c), _lib.ptr(w) if w is not None else None, _lib.ptr(ev), etype,
+                                  _lib.ptr(out), self.cluster, _lib.ptr(ws), ws_bytes, _lib.stream_handle(dev))
+    _lib.check(st, "event_csrmv_planned")
+    return out
+
+
+def prepare(indices, indptr, *, shape, data=None, tile_w=None, cluster=4) -> CSRPlan:
+  """Builds the tiled plan of a CSR matrix (heterogeneous when `data` has nse entries)."""
+  dev = indices.device if isinstance(indices, torch.Tensor) and indices.is_cuda else default_device()
+  indices = as_tensor(indices, dev)
+  indptr = as_tensor(indptr, dev)
+  d = None
+  if data is not None:
+    d = float_data(data, dev)
+  return CSRPlan(indices, indptr, shape, d, tile_w, cluster)
+
+
+# ---- automatic plan cache ---------------------------------------------------------
+# Keyed by the identity and version counter of the CSR tensors (and of heterogeneous
+# weights), so an in-place change of any of them invalidates the entry.
+_PLANS = {}
+_PLAN_MIN_N = int(os.environ.get("BPGPU_PLAN_MIN_N", 1 << 15))
+_PLAN_MIN_NNZ = int(os.environ.get("BPGPU_PLAN_MIN_NNZ", 1 << 20))
+_PLAN_DISABLE = os.environ.get("BPGPU_DISABLE_PLAN", "0") == "1"
+
+
+def _plan_key(t):
+  return (id(t), t.data_ptr(), t._version)
+
+
+def _cached_plan(data, indices, indptr, shape):
+  if _PLAN_DISABLE:
+    return None
+  m, n = int(shape[0]), int(shape[1])
+  if n < _PLAN_MIN_N or indices.numel() < _PLAN_MIN_NNZ:
+    return None
+  heter = data.numel() > 1
+  key = (_plan_key(indices), _plan_key(indptr), m, n, _plan_key(data) if heter else None)
+  ent = _PLANS.get(key)
+  if ent is not None:
+    refs, plan = ent
+    if all(r() is not None for r in refs):
+      return plan
+    del _PLANS[key]
+  for k in [k for k, (refs, _) in _PLANS.items() if any(r() is None for r in refs)]:
+    del _PLANS[k]
+  plan = CSRPlan(indices, indptr, (m, n), data if heter else None)
+  refs = [weakref.ref(indices), weakref.ref(indptr)] + ([weakref.ref(data)] if heter else [])
+  _PLANS[key] = (refs, plan)
+  return plan
 
 
 def _check_common(data, indices, indptr, events, shape, transpose):
@@ -52,6 +154,10 @@ def _event_csrmv(data, indices, indptr, events, shape, transpose, float_rule, ou
   etype, ev = event_type(events, float_rule)
   m, n = int(shape[0]), int(shape[1])
   n_out = n if transpose else m
+  if transpose:
+    plan = _cached_plan(data, indices, indptr, (m, n))
+    if plan is not None:
+      return plan.csrmv(events, None if plan.heter else data, out=out, float_rule=float_rule)
   if out is None:
     out = torch.empty(n_out, dtype=torch.float32, device=dev)
   L = _lib.lib()

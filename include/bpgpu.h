@@ -83,6 +83,45 @@ bp_status bp_event_csrmv(const float* data, int64_t ndata, const void* indices, 
                          size_t workspace_bytes, bp_stream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * Column-tiled CSR plan (no counterpart in the reference; it plays the role of a
+ * cuSPARSE-style analysis step).  A one-time re-layout of a CSR matrix that the tiled
+ * event kernels stream: every row's indices regrouped by column tile of tile_w columns,
+ * stored as tile-local uint16 and padded to 8-byte chunks, weights permuted along.
+ * The caller owns the device memory (bp_csr_plan_bytes) and keeps it, together with the
+ * filled-in bp_csr_plan, for as long as it uses the plan.  A plan is a function of
+ * (indices, indptr[, data]) at build time; rebuild it when they change.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  int64_t m, n, nnz;  /* matrix shape and number of stored entries */
+  int32_t tile_w;     /* columns per tile (<= 65535) */
+  int32_t n_tiles;    /* ceil(n / tile_w) */
+  int32_t heter;      /* 1: the plan carries permuted float32 weights */
+  int32_t reserved;
+  uint64_t entries;   /* capacity of the padded index array */
+  void* mem;          /* device memory holding the plan (caller-owned) */
+  size_t bytes;       /* size of mem */
+} bp_csr_plan;
+
+/* tile width the tiled kernels run best with on the current device for n columns and
+ * clusters of `cluster` CTAs (1, 2, 4 or 8); 0 on error. */
+int32_t bp_csr_plan_default_tile(int64_t n, int32_t cluster);
+size_t bp_csr_plan_bytes(int64_t m, int64_t n, int64_t nnz, int32_t heter, int32_t tile_w);
+/* Builds the plan on `stream` (heterogeneous when ndata == nnz > 1, homogeneous when
+ * data is NULL or ndata == 1). */
+bp_status bp_csr_plan_build(const float* data, int64_t ndata, const void* indices, const void* indptr,
+                            bp_itype itype, int64_t nnz, int64_t m, int64_t n, int32_t tile_w, void* mem,
+                            size_t bytes, bp_csr_plan* plan_out, bp_stream_t stream);
+
+/* event.csrmv, transpose=1, on a plan: out (n) = sum of the active rows.  `w_homo` is the
+ * homogeneous weight (device pointer to one float) for homogeneous plans and is ignored for
+ * heterogeneous ones.  `cluster` = CTAs per column tile (1, 2, 4, 8; 0 = default).
+ * Homogeneous: exact integer counts, out = (float)count * w. */
+size_t bp_event_csrmv_planned_workspace_size(const bp_csr_plan* plan);
+bp_status bp_event_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, const void* events, bp_etype etype,
+                                 float* out, int32_t cluster, void* workspace, size_t workspace_bytes,
+                                 bp_stream_t stream);
+
+/* ---------------------------------------------------------------------------
  * event.csrmv with no allocation anywhere (no counterpart in the reference).
  * For callers that can pass nothing but operands and the result buffer -- e.g. a legacy
  * XLA custom-call target, which gets its buffers from XLA and has no scratch allocator,

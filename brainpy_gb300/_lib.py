@@ -15,6 +15,9 @@ _LIB = None
 BP_OK, BP_EINVAL, BP_ESHAPE, BP_EDTYPE, BP_ENOMEM, BP_ETIMEOUT, BP_ECUDA, BP_ENOTSUP = range(8)
 BP_I32, BP_I64 = 0, 1
 BP_EV_BOOL, BP_EV_F32_POS, BP_EV_F32_NZ = 0, 1, 2
+BP_JC_HOMO, BP_JC_UNIFORM, BP_JC_NORMAL = 0, 1, 2
+BP_VEC_EVENT_BOOL, BP_VEC_EVENT_F32, BP_VEC_DENSE_F32 = 0, 1, 2
+BP_JC_TAICHI_GPU, BP_JC_TAICHI_CPU = 0, 1
 
 _c_i64 = ctypes.c_int64
 _c_i32 = ctypes.c_int32
@@ -33,12 +36,30 @@ SIGNATURES = {
     "bp_event_csrmv_workspace_size": (_c_size, [_c_i64, _c_i64, _c_i32]),
     "bp_event_csrmv": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_ptr, _c_i32, _c_i64, _c_i64,
                                 _c_i32, _c_ptr, _c_ptr, _c_size, _c_ptr]),
+    "bp_csrmv": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_ptr, _c_i64, _c_i64, _c_i32, _c_ptr,
+                          _c_ptr]),
+    "bp_csr_to_coo": (_c_i32, [_c_ptr, _c_i32, _c_i64, _c_i64, _c_ptr, _c_ptr]),
+    "bp_csr_to_dense": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_ptr, _c_ptr]),
+    "bp_jitconn_mv": (_c_i32, [_c_i32, _c_i32, _c_ptr, _c_i64, _c_i64, _c_f32, _c_f32, _c_i32, _c_u32, _c_i32, _c_i32,
+                               _c_ptr, _c_ptr]),
+    "bp_jitconn_dense": (_c_i32, [_c_i32, _c_f32, _c_f32, _c_i32, _c_u32, _c_i64, _c_i64, _c_i32, _c_i32, _c_ptr,
+                                  _c_ptr]),
     "bp_csr_plan_default_tile": (_c_i32, [_c_i64, _c_i32]),
     "bp_csr_plan_bytes": (_c_size, [_c_i64, _c_i64, _c_i64, _c_i32, _c_i32]),
     "bp_csr_plan_build": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_i32, _c_ptr,
                                    _c_size, _c_ptr, _c_ptr]),
     "bp_event_csrmv_planned_workspace_size": (_c_size, [_c_ptr]),
     "bp_event_csrmv_planned": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_i32, _c_ptr, _c_i32, _c_ptr, _c_size, _c_ptr]),
+    "bp_csrmv_planned": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i32, _c_ptr, _c_size, _c_ptr]),
+    "bp_csr_plan_arrays": (_c_i32, [_c_ptr, ctypes.POINTER(_c_ptr), ctypes.POINTER(_c_ptr), ctypes.POINTER(_c_ptr),
+                                    ctypes.POINTER(_c_ptr)]),
+    "bp_lif_coba_step": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i32,
+                                  _c_f32, _c_ptr]),
+    "bp_lif_coba_step_dev": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr,
+                                      _c_i32, _c_f32, _c_ptr]),
+    "bp_net_max_tiles": (_c_i32, []),
+    "bp_net_tile_width": (_c_i32, []),
+    "bp_net_run": (_c_i32, [_c_ptr, _c_i32, _c_i32, _c_i32, _c_i32, _c_f32, _c_ptr]),
     "bp_event_csrmv_noalloc_max_rows": (_c_i64, []),
     "bp_event_csrmv_noalloc": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_ptr, _c_i32, _c_i64,
                                         _c_i64, _c_i32, _c_ptr, _c_ptr]),
@@ -52,6 +73,22 @@ class CsrPlan(ctypes.Structure):
   _fields_ = [("m", _c_i64), ("n", _c_i64), ("nnz", _c_i64), ("tile_w", _c_i32), ("n_tiles", _c_i32),
               ("heter", _c_i32), ("reserved", _c_i32), ("entries", ctypes.c_uint64), ("mem", _c_ptr),
               ("bytes", _c_size)]
+
+
+class LifParams(ctypes.Structure):
+  """Mirror of bp_lif_params (include/bpgpu.h)."""
+  _fields_ = [("V_rest", _c_f32), ("V_th", _c_f32), ("V_reset", _c_f32), ("tau", _c_f32), ("tau_ref", _c_f32),
+              ("R", _c_f32), ("tau_e", _c_f32), ("tau_i", _c_f32), ("E_e", _c_f32), ("E_i", _c_f32),
+              ("input", _c_f32), ("ltc", _c_i32)]
+
+
+class NetDesc(ctypes.Structure):
+  """Mirror of bp_net_desc (include/bpgpu.h)."""
+  _fields_ = [("n", _c_i32), ("n_exc", _c_i32), ("tile_w", _c_i32), ("n_tiles", _c_i32),
+              ("row_start", _c_ptr), ("tile_off", _c_ptr), ("idx", _c_ptr), ("we", _c_f32), ("wi", _c_f32),
+              ("p", LifParams), ("V", _c_ptr), ("ge", _c_ptr), ("gi", _c_ptr), ("t_last", _c_ptr),
+              ("spike", _c_ptr), ("spike_counts", _c_ptr), ("raster", _c_ptr), ("v_trace", _c_ptr),
+              ("trace_steps", _c_i32), ("reserved", _c_i32)]
 
 
 class BPError(RuntimeError):

@@ -1,0 +1,212 @@
+// csrmv.cu -- sparse.csrmv on plain CSR (dense float32 vector).
+//
+// transpose=0: y[i] = sum_j A[i, j] x[j]   one warp per row, coalesced index/weight streaming,
+//              gathers of x, lane partials reduced in the warp (deterministic order).
+// transpose=1: y[j] = sum_i A[i, j] x[i]   one warp per row with x[i] != 0, red.global.add.f32.
+//              (bp_csrmv_planned is the shared-memory tiled form of the same product.)
+// Homogeneous weight: x values are summed and multiplied by w once per lane, as the reference's
+// Taichi GPU kernels do (brainpy/_src/math/sparse/_csr_mv_taichi.py:115-120, :124-135).
+// Reference semantics: brainpy/_src/math/sparse/_csr_mv.py:126-164 (Numba CPU).
+#include "common.cuh"
+#include "timer.cuh"
+
+namespace bp {
+
+template <typename IdxT>
+__device__ __forceinline__ void csr_row_bounds(const IdxT* indptr, int64_t row, int64_t nnz, int64_t& b, int64_t& e) {
+  b = (int64_t)indptr[row];
+  e = (int64_t)indptr[row + 1];
+  b = b < 0 ? 0 : (b > nnz ? nnz : b);
+  e = e < b ? b : (e > nnz ? nnz : e);
+}
+
+template <typename IdxT, bool HOMO>
+__global__ void __launch_bounds__(256) csrmv_n_kernel(const IdxT* __restrict__ indptr, const IdxT* __restrict__ indices,
+                                                      const float* __restrict__ data, int64_t nnz, int64_t m,
+                                                      int64_t n, const float* __restrict__ x, float* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < m; row += nwarps) {
+    int64_t b, e;
+    csr_row_bounds(indptr, row, nnz, b, e);
+    float acc = 0.0f;
+    int64_t j = b + lane;
+    for (; j + 96 < e; j += 128) {
+      int64_t c0 = (int64_t)indices[j], c1 = (int64_t)indices[j + 32];
+      int64_t c2 = (int64_t)indices[j + 64], c3 = (int64_t)indices[j + 96];
+      float x0 = (uint64_t)c0 < (uint64_t)n ? __ldg(x + c0) : 0.0f;
+      float x1 = (uint64_t)c1 < (uint64_t)n ? __ldg(x + c1) : 0.0f;
+      float x2 = (uint64_t)c2 < (uint64_t)n ? __ldg(x + c2) : 0.0f;
+      float x3 = (uint64_t)c3 < (uint64_t)n ? __ldg(x + c3) : 0.0f;
+      if (HOMO) {
+        acc += x0;
+        acc += x1;
+        acc += x2;
+        acc += x3;
+      } else {
+        acc = fmaf(data[j], x0, acc);
+        acc = fmaf(data[j + 32], x1, acc);
+        acc = fmaf(data[j + 64], x2, acc);
+        acc = fmaf(data[j + 96], x3, acc);
+      }
+    }
+    for (; j < e; j += 32) {
+      int64_t c = (int64_t)indices[j];
+      float xv = (uint64_t)c < (uint64_t)n ? __ldg(x + c) : 0.0f;
+      if (HOMO) acc += xv;
+      else acc = fmaf(data[j], xv, acc);
+    }
+    if (HOMO) acc *= __ldg(data);
+    acc = warp_sum(acc);
+    if (lane == 0) out[row] = acc;
+  }
+}
+
+template <typename IdxT, bool HOMO>
+__global__ void __launch_bounds__(256) csrmv_t_kernel(const IdxT* __restrict__ indptr, const IdxT* __restrict__ indices,
+                                                      const float* __restrict__ data, int64_t nnz, int64_t m,
+                                                      int64_t n, const float* __restrict__ x, float* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < m; row += nwarps) {
+    const float xv = __ldg(x + row);
+    if (xv == 0.0f) continue;  // warp-uniform: the row adds nothing
+    int64_t b, e;
+    csr_row_bounds(indptr, row, nnz, b, e);
+    const float wx = HOMO ? __fmul_rn(__ldg(data), xv) : 0.0f;
+    for (int64_t j = b + lane; j < e; j += 32) {
+      int64_t c = (int64_t)indices[j];
+      if ((uint64_t)c < (uint64_t)n) atomicAdd(out + c, HOMO ? wx : __fmul_rn(data[j], xv));
+    }
+  }
+}
+
+// CSR -> COO rows (brainpy/_src/math/sparse/_utils.py:44-52): rows[j] = i for j in row i
+template <typename IdxT>
+__global__ void __launch_bounds__(256) csr_rows_kernel(const IdxT* __restrict__ indptr, int64_t m, int64_t nnz,
+                                                       IdxT* __restrict__ rows) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < m; row += nwarps) {
+    int64_t b, e;
+    csr_row_bounds(indptr, row, nnz, b, e);
+    for (int64_t j = b + lane; j < e; j += 32) rows[j] = (IdxT)row;
+  }
+}
+
+// CSR -> dense (brainpy/_src/math/sparse/_utils.py:70-81 and :101-114): duplicates add up
+template <typename IdxT>
+__global__ void __launch_bounds__(256) csr_dense_kernel(const float* __restrict__ data, int homo,
+                                                        const IdxT* __restrict__ indptr, const IdxT* __restrict__ indices,
+                                                        int64_t m, int64_t n, int64_t nnz, float* __restrict__ dense) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < m; row += nwarps) {
+    int64_t b, e;
+    csr_row_bounds(indptr, row, nnz, b, e);
+    for (int64_t j = b + lane; j < e; j += 32) {
+      const int64_t c = (int64_t)indices[j];
+      if ((uint64_t)c < (uint64_t)n) atomicAdd(dense + row * n + c, homo ? __ldg(data) : data[j]);
+    }
+  }
+}
+
+static int grid_rows(int64_t m) {
+  int64_t g = (m + 7) / 8;
+  const int64_t maxb = (int64_t)device_sm_count() * 32;
+  if (g < 1) g = 1;
+  return (int)(g > maxb ? maxb : g);
+}
+
+template <typename IdxT>
+static bp_status csrmv_dispatch(const float* data, bool homo, const IdxT* indices, const IdxT* indptr, int64_t nnz,
+                                const float* x, int64_t m, int64_t n, int transpose, float* out, cudaStream_t st) {
+  const int g = grid_rows(m);
+  ScopedKernelTimer tk(st);
+  if (transpose) {
+    BP_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * (size_t)n, st));
+    if (homo) csrmv_t_kernel<IdxT, true><<<g, 256, 0, st>>>(indptr, indices, data, nnz, m, n, x, out);
+    else csrmv_t_kernel<IdxT, false><<<g, 256, 0, st>>>(indptr, indices, data, nnz, m, n, x, out);
+  } else {
+    if (homo) csrmv_n_kernel<IdxT, true><<<g, 256, 0, st>>>(indptr, indices, data, nnz, m, n, x, out);
+    else csrmv_n_kernel<IdxT, false><<<g, 256, 0, st>>>(indptr, indices, data, nnz, m, n, x, out);
+  }
+  return check_launch("csrmv kernel");
+}
+
+}  // namespace bp
+
+using namespace bp;
+
+extern "C" {
+
+bp_status bp_csrmv(const float* data, int64_t ndata, const void* indices, const void* indptr, bp_itype itype,
+                   int64_t nnz, const float* vec, int64_t m, int64_t n, int32_t transpose, float* out,
+                   bp_stream_t stream) {
+  clear_error();
+  cudaStream_t st = as_cuda(stream);
+  BP_REQUIRE(m >= 0 && n >= 0 && nnz >= 0, BP_EINVAL, "csrmv: negative size");
+  BP_REQUIRE(m <= INT32_MAX && n <= INT32_MAX, BP_ENOTSUP, "csrmv: dimensions beyond int32 range");
+  BP_REQUIRE(itype == BP_I32 || itype == BP_I64, BP_EDTYPE, "csrmv: bad index type %d", (int)itype);
+  BP_REQUIRE(ndata == 1 || ndata == nnz, BP_ESHAPE,
+             "csrmv: the size of data should be 1 or be consistent with indices (%lld vs %lld)", (long long)ndata,
+             (long long)nnz);
+  const int64_t n_out = transpose ? n : m;
+  if (n_out == 0) return BP_OK;
+  BP_REQUIRE(out != nullptr, BP_EINVAL, "csrmv: null out");
+  if (m == 0 || nnz == 0) {
+    BP_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * (size_t)n_out, st));
+    return BP_OK;
+  }
+  BP_REQUIRE(data && indices && indptr && vec, BP_EINVAL, "csrmv: null data/indices/indptr/vector");
+  const bool homo = ndata == 1;
+  if (itype == BP_I32)
+    return csrmv_dispatch<int32_t>(data, homo, static_cast<const int32_t*>(indices), static_cast<const int32_t*>(indptr),
+                                   nnz, vec, m, n, transpose, out, st);
+  return csrmv_dispatch<int64_t>(data, homo, static_cast<const int64_t*>(indices), static_cast<const int64_t*>(indptr),
+                                 nnz, vec, m, n, transpose, out, st);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+bp_status bp_csr_to_coo(const void* indptr, bp_itype itype, int64_t m, int64_t nnz, void* rows, bp_stream_t stream) {
+  clear_error();
+  cudaStream_t st = as_cuda(stream);
+  BP_REQUIRE(m >= 0 && nnz >= 0, BP_EINVAL, "csr_to_coo: negative size");
+  BP_REQUIRE(itype == BP_I32 || itype == BP_I64, BP_EDTYPE, "csr_to_coo: bad index type");
+  if (m == 0 || nnz == 0) return BP_OK;
+  BP_REQUIRE(indptr && rows, BP_EINVAL, "csr_to_coo: null pointer");
+  const int g = grid_rows(m);
+  if (itype == BP_I32)
+    csr_rows_kernel<int32_t><<<g, 256, 0, st>>>(static_cast<const int32_t*>(indptr), m, nnz, static_cast<int32_t*>(rows));
+  else
+    csr_rows_kernel<int64_t><<<g, 256, 0, st>>>(static_cast<const int64_t*>(indptr), m, nnz, static_cast<int64_t*>(rows));
+  return check_launch("csr_rows_kernel");
+}
+
+bp_status bp_csr_to_dense(const float* data, int64_t ndata, const void* indices, const void* indptr, bp_itype itype,
+                          int64_t nnz, int64_t m, int64_t n, float* dense, bp_stream_t stream) {
+  clear_error();
+  cudaStream_t st = as_cuda(stream);
+  BP_REQUIRE(m >= 0 && n >= 0 && nnz >= 0, BP_EINVAL, "csr_to_dense: negative size");
+  BP_REQUIRE(itype == BP_I32 || itype == BP_I64, BP_EDTYPE, "csr_to_dense: bad index type");
+  BP_REQUIRE(ndata == 1 || ndata == nnz, BP_ESHAPE, "csr_to_dense: data size %lld vs nnz %lld", (long long)ndata,
+             (long long)nnz);
+  if (m == 0 || n == 0) return BP_OK;
+  BP_REQUIRE(dense != nullptr, BP_EINVAL, "csr_to_dense: null output");
+  BP_CUDA_TRY(cudaMemsetAsync(dense, 0, sizeof(float) * (size_t)m * (size_t)n, st));
+  if (nnz == 0) return BP_OK;
+  BP_REQUIRE(data && indices && indptr, BP_EINVAL, "csr_to_dense: null pointer");
+  const int g = grid_rows(m);
+  if (itype == BP_I32)
+    csr_dense_kernel<int32_t><<<g, 256, 0, st>>>(data, ndata == 1, static_cast<const int32_t*>(indptr),
+                                                 static_cast<const int32_t*>(indices), m, n, nnz, dense);
+  else
+    csr_dense_kernel<int64_t><<<g, 256, 0, st>>>(data, ndata == 1, static_cast<const int64_t*>(indptr),
+                                                 static_cast<const int64_t*>(indices), m, n, nnz, dense);
+  return check_launch("csr_dense_kernel");
+}
+
+}  // extern "C"

@@ -141,15 +141,24 @@ __device__ __forceinline__ uint2 ld_stream_u2(const uint16_t* p) {
 }
 __device__ __forceinline__ float4 ld_stream_f4(const float* p) { return __ldcs(reinterpret_cast<const float4*>(p)); }
 
-template <bool HOMO>
-__device__ __forceinline__ void accumulate4(uint32_t* acc, uint2 v, float4 wv, uint32_t tile_w) {
+// Accumulation modes of the tiled kernel:
+//   kCount  homogeneous weight, events: uint32 event counts, out = (float)count * w
+//   kWeight heterogeneous weights, events: float32 sum of w_ij
+//   kRowVal homogeneous weight, dense vector x: float32 sum of x_i, out = w * sum
+//   kWRow   heterogeneous weights, dense vector x: float32 sum of w_ij * x_i
+enum { kCount = 0, kWeight = 1, kRowVal = 2, kWRow = 3 };
+
+template <int MODE>
+__device__ __forceinline__ void accumulate4(uint32_t* acc, uint2 v, float4 wv, float xv, uint32_t tile_w) {
   uint32_t x[4] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16};
   float ww[4] = {wv.x, wv.y, wv.z, wv.w};
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     if (x[q] < tile_w) {  // excludes the 0xFFFF padding
-      if (HOMO) atomicAdd(acc + x[q], 1u);
-      else atomicAdd(reinterpret_cast<float*>(acc) + x[q], ww[q]);
+      if (MODE == kCount) atomicAdd(acc + x[q], 1u);
+      else if (MODE == kWeight) atomicAdd(reinterpret_cast<float*>(acc) + x[q], ww[q]);
+      else if (MODE == kRowVal) atomicAdd(reinterpret_cast<float*>(acc) + x[q], xv);
+      else atomicAdd(reinterpret_cast<float*>(acc) + x[q], __fmul_rn(ww[q], xv));
     }
   }
 }
@@ -162,6 +171,7 @@ struct TiledArgs {
   const int32_t* lists;
   const int32_t* counts;
   const float* w_homo;
+  const float* row_val;  // dense vector for kRowVal / kWRow
   float* out;
   int64_t n;
   int32_t tile_w, n_tiles, nb, acc_words;
@@ -174,8 +184,10 @@ struct TiledArgs {
 // and the descriptors of slice k+W are in flight while slice k is processed.  Inside a slice,
 // groups of G lanes take one segment each (lane gl loads 8-byte chunk gl, 4 uint16 indices)
 // and G segments are loaded back to back before any shared-memory atomic is issued.
-template <bool HOMO>
+template <int MODE>
 __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArgs a) {
+  constexpr bool HAS_W = (MODE == kWeight || MODE == kWRow);
+  constexpr bool HAS_X = (MODE == kRowVal || MODE == kWRow);
   extern __shared__ uint4 smem_raw[];
   uint32_t* acc = reinterpret_cast<uint32_t*>(smem_raw);
   int* s_boff = reinterpret_cast<int*>(acc + a.acc_words);  // kBlockGroup + 1
@@ -246,10 +258,12 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArg
       }
       return lo;
     };
-    auto fetch_desc = [&](int32_t row, uint32_t& st, uint32_t& nch) {
+    auto fetch_desc = [&](int32_t row, uint32_t& st, uint32_t& nch, float& xv) {
       st = 0;
       nch = 0;
+      xv = 0.0f;
       if (row >= 0) {
+        if (HAS_X) xv = __ldg(a.row_val + row);
         const uint64_t rs = __ldg(row_start + row);
         const uint32_t* to = tile_off + (int64_t)row * toff_stride + tile;
         const uint32_t o0 = __ldg(to), o1 = __ldg(to + 1);
@@ -261,20 +275,22 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArg
     int k = warp;
     int blk1 = block_of(min((k << 5) + lane, max(total - 1, 0)));
     uint32_t cst, cn;
-    fetch_desc(fetch_row(k, blk1), cst, cn);
+    float cxv;
+    fetch_desc(fetch_row(k, blk1), cst, cn, cxv);
     int blk2 = block_of(min(((k + nwarps) << 5) + lane, max(total - 1, 0)));
     int32_t row1 = fetch_row(k + nwarps, blk2);
     int blk3 = blk2;
     while (k < nslices) {
       uint32_t nst, nn;
-      fetch_desc(row1, nst, nn);  // slice k + W: in flight during slice k
+      float nxv;
+      fetch_desc(row1, nst, nn, nxv);  // slice k + W: in flight during slice k
       int32_t row2 = -1;
       if (k + 2 * nwarps < nslices) {
         blk3 = block_of(min(((k + 2 * nwarps) << 5) + lane, max(total - 1, 0)));
         row2 = fetch_row(k + 2 * nwarps, blk3);
       }
       // this lane's segment: chunks [0, cn) at entry cst; U chunk loads before the atomics
-      constexpr int U = HOMO ? 8 : 4;
+      constexpr int U = HAS_W ? 4 : 8;
       for (uint32_t c0 = 0; __any_sync(0xffffffffu, c0 < cn); c0 += U) {
         uint2 vv[U];
         float4 wv[U];
@@ -283,15 +299,16 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArg
           if (c0 + u < cn) {
             const uint32_t e = cst + 4u * (c0 + u);
             vv[u] = ld_stream_u2(a.idx + e);
-            if (!HOMO) wv[u] = ld_stream_f4(a.w + e);
+            if (HAS_W) wv[u] = ld_stream_f4(a.w + e);
           }
         }
 #pragma unroll
         for (int u = 0; u < U; ++u)
-          if (c0 + u < cn) accumulate4<HOMO>(acc, vv[u], HOMO ? make_float4(0, 0, 0, 0) : wv[u], a.tile_w);
+          if (c0 + u < cn) accumulate4<MODE>(acc, vv[u], HAS_W ? wv[u] : make_float4(0, 0, 0, 0), cxv, a.tile_w);
       }
       cst = nst;
       cn = nn;
+      cxv = nxv;
       row1 = row2;
       k += nwarps;
     }
@@ -301,11 +318,11 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArg
   cluster.sync();
   const int slice = a.acc_words / R;  // multiple of 4
   const int c0 = rank * slice;
-  const float w = HOMO ? __ldg(a.w_homo) : 0.0f;
+  const float w = (MODE == kCount || MODE == kRowVal) ? __ldg(a.w_homo) : 0.0f;
   const int64_t col_base = (int64_t)tile * a.tile_w;
   for (int c = c0 + 4 * tid; c < c0 + slice; c += 4 * nthr) {
     float o[4];
-    if (HOMO) {
+    if (MODE == kCount) {
       uint4 s = make_uint4(0, 0, 0, 0);
       for (int r = 0; r < R; ++r) {
         const uint4 x = *reinterpret_cast<const uint4*>(cluster.map_shared_rank(acc, r) + c);
@@ -326,6 +343,12 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArg
         s.y += x.y;
         s.z += x.z;
         s.w += x.w;
+      }
+      if (MODE == kRowVal) {
+        s.x = __fmul_rn(w, s.x);
+        s.y = __fmul_rn(w, s.y);
+        s.z = __fmul_rn(w, s.z);
+        s.w = __fmul_rn(w, s.w);
       }
       o[0] = s.x;
       o[1] = s.y;
@@ -352,9 +375,9 @@ static int acc_words_for(int tile_w, int R) {
   return (tile_w + q - 1) / q * q;
 }
 
-template <bool HOMO>
+template <int MODE>
 static bp_status launch_tiled(const TiledArgs& a, int R, cudaStream_t st) {
-  auto kfn = ecsr_t_tiled_kernel<HOMO>;
+  auto kfn = ecsr_t_tiled_kernel<MODE>;
   const size_t smem = tiled_smem_bytes(a.acc_words);
   static thread_local size_t configured[64] = {0};
   int dev = 0;
@@ -402,7 +425,7 @@ static bp_status compact_blocked(const void* events, bp_etype et, int64_t m, int
 }
 
 static int max_active_clusters(int R, size_t smem) {
-  auto kfn = ecsr_t_tiled_kernel<true>;
+  auto kfn = ecsr_t_tiled_kernel<kCount>;
   if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   cudaLaunchConfig_t cfg = {};
@@ -524,6 +547,18 @@ bp_status bp_csr_plan_build(const float* data, int64_t ndata, const void* indice
   return BP_OK;
 }
 
+bp_status bp_csr_plan_arrays(const bp_csr_plan* plan, const uint64_t** row_start, const uint32_t** tile_off,
+                             const uint16_t** idx, const float** w) {
+  clear_error();
+  BP_REQUIRE(plan != nullptr && plan->mem != nullptr, BP_EINVAL, "csr_plan_arrays: null plan");
+  PlanView v = plan_view(plan);
+  if (row_start) *row_start = v.row_start;
+  if (tile_off) *tile_off = v.tile_off;
+  if (idx) *idx = v.idx;
+  if (w) *w = v.w;
+  return BP_OK;
+}
+
 size_t bp_event_csrmv_planned_workspace_size(const bp_csr_plan* plan) {
   if (!plan || plan->m <= 0) return 256;
   int64_t nb = (plan->m + kCompactRows - 1) / kCompactRows;
@@ -573,6 +608,7 @@ bp_status bp_event_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, c
   a.lists = lists;
   a.counts = counts;
   a.w_homo = w_homo;
+  a.row_val = nullptr;
   a.out = out;
   a.n = n;
   a.tile_w = plan->tile_w;
@@ -580,8 +616,65 @@ bp_status bp_event_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, c
   a.nb = nb;
   a.acc_words = acc_words;
   a.vec_out = ((reinterpret_cast<uintptr_t>(out) & 15u) == 0) ? 1 : 0;
-  s = homo ? launch_tiled<true>(a, cluster, st) : launch_tiled<false>(a, cluster, st);
+  s = homo ? launch_tiled<kCount>(a, cluster, st) : launch_tiled<kWeight>(a, cluster, st);
   return s;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// sparse.csrmv, transpose=1, on a plan: out[j] = sum_i A[i, j] * vec[i].  Rows with vec[i] == 0
+// contribute nothing and are skipped by the compaction (the dense vector is treated as
+// events under the != 0 rule); the others carry their value into the tile accumulation.
+bp_status bp_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, const float* vec, float* out,
+                           int32_t cluster, void* workspace, size_t workspace_bytes, bp_stream_t stream) {
+  clear_error();
+  cudaStream_t st = as_cuda(stream);
+  BP_REQUIRE(plan != nullptr && plan->mem != nullptr, BP_EINVAL, "csrmv_planned: null plan");
+  if (cluster == 0) cluster = 4;
+  BP_REQUIRE(cluster == 1 || cluster == 2 || cluster == 4 || cluster == 8, BP_EINVAL,
+             "csrmv_planned: cluster must be 1, 2, 4 or 8 (got %d)", cluster);
+  const int64_t m = plan->m, n = plan->n;
+  if (n == 0) return BP_OK;
+  BP_REQUIRE(out != nullptr, BP_EINVAL, "csrmv_planned: null out");
+  if (m == 0 || plan->nnz == 0) {
+    BP_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * (size_t)n, st));
+    return BP_OK;
+  }
+  BP_REQUIRE(vec != nullptr, BP_EINVAL, "csrmv_planned: null vector");
+  const bool homo = plan->heter == 0;
+  BP_REQUIRE(!homo || w_homo != nullptr, BP_EINVAL, "csrmv_planned: homogeneous plan needs w_homo");
+  BP_REQUIRE(workspace && workspace_bytes >= bp_event_csrmv_planned_workspace_size(plan), BP_ENOMEM,
+             "csrmv_planned: workspace %zu < %zu", workspace_bytes, bp_event_csrmv_planned_workspace_size(plan));
+  const int acc_words = acc_words_for(plan->tile_w, cluster);
+  BP_REQUIRE(tiled_smem_bytes(acc_words) <= (size_t)max_smem_optin(), BP_ENOTSUP,
+             "csrmv_planned: tile of %d columns does not fit shared memory", plan->tile_w);
+  const int nb = (int)((m + kCompactRows - 1) / kCompactRows);
+  int32_t* lists = static_cast<int32_t*>(workspace);
+  int32_t* counts = reinterpret_cast<int32_t*>(static_cast<char*>(workspace) +
+                                               align_up(sizeof(int32_t) * (size_t)nb * kCompactRows, 256));
+  ScopedKernelTimer tk(st);
+  bp_status s = compact_blocked(vec, BP_EV_F32_NZ, m, lists, counts, st);
+  if (s != BP_OK) return s;
+  PlanView v = plan_view(plan);
+  TiledArgs a;
+  a.row_start = v.row_start;
+  a.tile_off = v.tile_off;
+  a.idx = v.idx;
+  a.w = v.w;
+  a.lists = lists;
+  a.counts = counts;
+  a.w_homo = w_homo;
+  a.row_val = vec;
+  a.out = out;
+  a.n = n;
+  a.tile_w = plan->tile_w;
+  a.n_tiles = plan->n_tiles;
+  a.nb = nb;
+  a.acc_words = acc_words;
+  a.vec_out = ((reinterpret_cast<uintptr_t>(out) & 15u) == 0) ? 1 : 0;
+  return homo ? launch_tiled<kRowVal>(a, cluster, st) : launch_tiled<kWRow>(a, cluster, st);
 }
 
 }  // extern "C"

@@ -1,0 +1,263 @@
+// net.cu -- LIF/Expon/COBA neuron update and whole-network persistent simulation.
+//
+// bp_lif_coba_step: one thread per neuron, the per-operator building block.
+//
+// bp_net_run: E/I COBA networks of up to 16 x 4096 neurons, each simulated by one thread-block
+// cluster for many steps inside a single launch.  CTA `rank` owns neurons
+// [rank*tile_w, (rank+1)*tile_w): their state, their two conductance event counters and the
+// list of their spikes live in shared memory.  Step s:
+//   1. propagation of step s-1's spikes: every CTA reads all ranks' spike lists through
+//      distributed shared memory and, for each spiking row, streams that row's plan segment for
+//      its own tile (tile-local uint16 indices), counting events per post-synaptic neuron with
+//      shared-memory atomics, separately for excitatory and inhibitory rows;
+//   2. neuron update with dge = count_e * we, dgi = count_i * wi; new spikes go into the other
+//      half of a double-buffered list;
+//   3. one cluster barrier.
+// Reference order of a step (align_post.py:271-275, lif.py:461-500): the projections add the
+// previous step's spike currents to the conductances, then the neurons update.
+#include <cooperative_groups.h>
+
+#include "common.cuh"
+#include "lif.cuh"
+#include "timer.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace bp {
+
+constexpr int kNetTileW = 4096;
+constexpr int kNetMaxTiles = 16;
+constexpr int kNetThreads = 1024;
+
+__global__ void __launch_bounds__(256) lif_step_kernel(bp_lif_params p, int64_t n, float* __restrict__ V,
+                                                       float* __restrict__ ge, float* __restrict__ gi,
+                                                       float* __restrict__ t_last, uint8_t* __restrict__ spike,
+                                                       const float* __restrict__ dge, const float* __restrict__ dgi,
+                                                       int32_t step, const int32_t* __restrict__ step_dev, float dt) {
+  const int32_t i = step_dev ? __ldg(step_dev) + step : step;
+  const float t = __fmul_rn((float)i, dt);
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    LifState s{V[k], ge[k], gi[k], t_last[k]};
+    const bool sp = lif_coba_update(p, s, dge ? dge[k] : 0.0f, dgi ? dgi[k] : 0.0f, t, dt);
+    V[k] = s.V;
+    ge[k] = s.ge;
+    gi[k] = s.gi;
+    t_last[k] = s.t_last;
+    spike[k] = sp ? 1 : 0;
+  }
+}
+
+struct NetSmem {
+  float V[kNetTileW], ge[kNetTileW], gi[kNetTileW], tl[kNetTileW];
+  uint32_t acc_e[kNetTileW], acc_i[kNetTileW];
+  int32_t list[2][kNetTileW];
+  int32_t cnt[2];
+};
+
+__global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_net_desc* __restrict__ descs,
+                                                                     int32_t step0, int32_t steps, float dt) {
+  extern __shared__ uint4 smem_raw[];
+  NetSmem& S = *reinterpret_cast<NetSmem*>(smem_raw);
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  const bp_net_desc d = descs[blockIdx.x / C];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const int tw = d.tile_w;
+  const int base = rank * tw;
+  const int nloc = max(0, min(tw, d.n - base));
+  const int words = (d.n + 31) >> 5;
+  const int64_t toff_stride = d.n_tiles + 1;
+
+  // load state, zero counters, initial spike list
+  if (tid < 2) S.cnt[tid] = 0;
+  for (int k = tid; k < tw; k += blockDim.x) {
+    const bool in = k < nloc;
+    S.V[k] = in ? d.V[base + k] : 0.0f;
+    S.ge[k] = in ? d.ge[base + k] : 0.0f;
+    S.gi[k] = in ? d.gi[base + k] : 0.0f;
+    S.tl[k] = in ? d.t_last[base + k] : 0.0f;
+    S.acc_e[k] = 0u;
+    S.acc_i[k] = 0u;
+  }
+  __syncthreads();
+  for (int k0 = 0; k0 < tw; k0 += blockDim.x) {
+    const int k = k0 + tid;
+    const bool sp = k < nloc && d.spike[base + k];
+    const unsigned m = __ballot_sync(0xffffffffu, sp);
+    int pos = 0;
+    if (lane == 0 && m) pos = atomicAdd(&S.cnt[0], __popc(m));
+    pos = __shfl_sync(0xffffffffu, pos, 0);
+    if (sp) S.list[0][pos + __popc(m & ((1u << lane) - 1u))] = k;
+  }
+  cluster.sync();
+
+  for (int s = 0; s < steps; ++s) {
+    const int cur = s & 1, nxt = cur ^ 1;
+    // ---- 1. propagate the previous step's spikes into this tile's counters
+    int pre[kNetMaxTiles + 1];
+    pre[0] = 0;
+    for (int r = 0; r < C; ++r) pre[r + 1] = pre[r] + *cluster.map_shared_rank(&S.cnt[cur], r);
+    const int total = pre[C];
+    for (int g0 = warp * 32; g0 < total; g0 += nwarps * 32) {
+      const int g = g0 + lane;
+      uint32_t st = 0, nch = 0;
+      bool exc = false;
+      if (g < total) {
+        int r = 0;
+        while (pre[r + 1] <= g) ++r;
+        const int32_t kloc = *cluster.map_shared_rank(&S.list[cur][g - pre[r]], r);
+        const int64_t row = (int64_t)r * tw + kloc;
+        exc = row < d.n_exc;
+        const uint64_t rs = __ldg(d.row_start + row);
+        const uint32_t* to = d.tile_off + row * toff_stride + rank;
+        const uint32_t o0 = __ldg(to), o1 = __ldg(to + 1);
+        st = (uint32_t)(rs + o0);
+        nch = (o1 - o0) >> 2;
+      }
+      uint32_t* acc = exc ? S.acc_e : S.acc_i;
+      constexpr int U = 8;
+      for (uint32_t c0 = 0; __any_sync(0xffffffffu, c0 < nch); c0 += U) {
+        uint2 vv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          if (c0 + u < nch) vv[u] = __ldg(reinterpret_cast<const uint2*>(d.idx + st + 4u * (c0 + u)));
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (c0 + u < nch) {
+            const uint32_t x[4] = {vv[u].x & 0xFFFFu, vv[u].x >> 16, vv[u].y & 0xFFFFu, vv[u].y >> 16};
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              if (x[q] < (uint32_t)nloc) atomicAdd(acc + x[q], 1u);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // ---- 2. neuron update
+    const float t = __fmul_rn((float)(step0 + s), dt);
+    if (tid == 0) S.cnt[nxt] = 0;
+    __syncthreads();
+    for (int k0 = 0; k0 < tw; k0 += blockDim.x) {
+      const int k = k0 + tid;
+      bool sp = false;
+      if (k < nloc) {
+        LifState st{S.V[k], S.ge[k], S.gi[k], S.tl[k]};
+        const float dge = __fmul_rn((float)S.acc_e[k], d.we);
+        const float dgi = __fmul_rn((float)S.acc_i[k], d.wi);
+        S.acc_e[k] = 0u;
+        S.acc_i[k] = 0u;
+        sp = lif_coba_update(d.p, st, dge, dgi, t, dt);
+        S.V[k] = st.V;
+        S.ge[k] = st.ge;
+        S.gi[k] = st.gi;
+        S.tl[k] = st.t_last;
+        if (d.v_trace && s < d.trace_steps) d.v_trace[(int64_t)s * d.n + base + k] = st.V;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, sp);
+      if (d.raster && lane == 0 && k - lane < nloc)
+        d.raster[(int64_t)s * words + ((base + k - lane) >> 5)] = m;
+      int pos = 0;
+      if (lane == 0 && m) pos = atomicAdd(&S.cnt[nxt], __popc(m));
+      pos = __shfl_sync(0xffffffffu, pos, 0);
+      if (sp) S.list[nxt][pos + __popc(m & ((1u << lane) - 1u))] = k;
+    }
+    __syncthreads();
+    if (tid == 0 && d.spike_counts && S.cnt[nxt]) atomicAdd(d.spike_counts + s, S.cnt[nxt]);
+    cluster.sync();
+  }
+
+  // write back state and the last step's spikes
+  const int last = steps & 1;
+  for (int k = tid; k < nloc; k += blockDim.x) {
+    d.V[base + k] = S.V[k];
+    d.ge[base + k] = S.ge[k];
+    d.gi[base + k] = S.gi[k];
+    d.t_last[base + k] = S.tl[k];
+    d.spike[base + k] = 0;
+  }
+  __syncthreads();
+  for (int j = tid; j < S.cnt[last]; j += blockDim.x) d.spike[base + S.list[last][j]] = 1;
+  cluster.sync();  // no CTA leaves while another may still read its lists
+}
+
+}  // namespace bp
+
+using namespace bp;
+
+extern "C" {
+
+bp_status bp_lif_coba_step(const bp_lif_params* params, int64_t n, float* V, float* ge, float* gi, float* t_last,
+                           uint8_t* spike, const float* dge, const float* dgi, int32_t step, float dt,
+                           bp_stream_t stream) {
+  clear_error();
+  cudaStream_t st = as_cuda(stream);
+  BP_REQUIRE(params != nullptr, BP_EINVAL, "lif_coba_step: null params");
+  BP_REQUIRE(n >= 0, BP_EINVAL, "lif_coba_step: negative size");
+  if (n == 0) return BP_OK;
+  BP_REQUIRE(V && ge && gi && t_last && spike, BP_EINVAL, "lif_coba_step: null state");
+  int64_t g = (n + 255) / 256;
+  const int64_t maxb = (int64_t)device_sm_count() * 16;
+  if (g > maxb) g = maxb;
+  ScopedKernelTimer tk(st);
+  lif_step_kernel<<<(int)g, 256, 0, st>>>(*params, n, V, ge, gi, t_last, spike, dge, dgi, step, nullptr, dt);
+  return check_launch("lif_step_kernel");
+}
+
+bp_status bp_lif_coba_step_dev(const bp_lif_params* params, int64_t n, float* V, float* ge, float* gi,
+                               float* t_last, uint8_t* spike, const float* dge, const float* dgi,
+                               const int32_t* step_dev, int32_t step_offset, float dt, bp_stream_t stream) {
+  clear_error();
+  cudaStream_t st = as_cuda(stream);
+  BP_REQUIRE(params != nullptr && step_dev != nullptr, BP_EINVAL, "lif_coba_step_dev: null params/step");
+  BP_REQUIRE(n >= 0, BP_EINVAL, "lif_coba_step_dev: negative size");
+  if (n == 0) return BP_OK;
+  BP_REQUIRE(V && ge && gi && t_last && spike, BP_EINVAL, "lif_coba_step_dev: null state");
+  int64_t g = (n + 255) / 256;
+  const int64_t maxb = (int64_t)device_sm_count() * 16;
+  if (g > maxb) g = maxb;
+  lif_step_kernel<<<(int)g, 256, 0, st>>>(*params, n, V, ge, gi, t_last, spike, dge, dgi, step_offset, step_dev, dt);
+  return check_launch("lif_step_kernel");
+}
+
+int32_t bp_net_max_tiles(void) { return kNetMaxTiles; }
+int32_t bp_net_tile_width(void) { return kNetTileW; }
+
+bp_status bp_net_run(const bp_net_desc* descs_device, int32_t num_nets, int32_t cluster, int32_t step0,
+                     int32_t steps, float dt, bp_stream_t stream) {
+  clear_error();
+  cudaStream_t st = as_cuda(stream);
+  BP_REQUIRE(num_nets >= 0 && steps >= 0, BP_EINVAL, "net_run: negative count");
+  BP_REQUIRE(cluster >= 1 && cluster <= kNetMaxTiles, BP_EINVAL, "net_run: cluster %d outside [1, %d]", cluster,
+             kNetMaxTiles);
+  if (num_nets == 0 || steps == 0) return BP_OK;
+  BP_REQUIRE(descs_device != nullptr, BP_EINVAL, "net_run: null descriptors");
+  auto kfn = net_cluster_kernel;
+  const size_t smem = sizeof(NetSmem);
+  static int configured[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!configured[dev]) {
+    BP_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    BP_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    configured[dev] = 1;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(num_nets * cluster), 1, 1);
+  cfg.blockDim = dim3(kNetThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  ScopedKernelTimer tk(st);
+  BP_CUDA_TRY(cudaLaunchKernelEx(&cfg, kfn, descs_device, step0, steps, dt));
+  return BP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,267 @@
+"""E/I COBA LIF networks on GB300: the consumer of the propagation operators.
+
+Mirrors examples/dynamics_simulation/COBA.py:58-109 (EICOBA_PostAlign): LifRefLTC / LifRef
+neurons (brainpy/_src/dyn/neurons/lif.py:348-556), Expon conductances with COBA outputs
+(dyn/synapses/abstract_models.py:24-134, dyn/outs/outputs.py:16-54), four event-driven
+projections E2E, E2I, I2E, I2I aligned post (dyn/projections/align_post.py:149-282), run by
+a DSRunner-style loop (brainpy/_src/runners.py:619-665).
+
+Two execution forms:
+* ``run(..., method="cluster")``: the whole run inside one persistent launch
+  (bp_net_run); the network must fit one thread-block cluster (n <= 16 x 4096).
+* ``run(..., method="ops")``: one event.csrmv / jitconn call per projection and one
+  neuron-update kernel per step (the per-operator path), optionally captured as a CUDA graph.
+"""
+import ctypes
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from .connect import fixed_prob_csr
+from .math import event as _event
+from .math import jitconn as _jitconn
+
+
+@dataclass
+class LifParams:
+  """Parameters of COBA.py's neurons and synapses (defaults: the example's values)."""
+  V_rest: float = -60.0
+  V_th: float = -50.0
+  V_reset: float = -60.0
+  tau: float = 20.0
+  tau_ref: float = 5.0
+  R: float = 1.0
+  tau_e: float = 5.0
+  tau_i: float = 10.0
+  E_e: float = 0.0
+  E_i: float = -80.0
+  input: float = 20.0
+  ltc: bool = True
+
+  def c(self):
+    return _lib.LifParams(self.V_rest, self.V_th, self.V_reset, self.tau, self.tau_ref, self.R, self.tau_e,
+                          self.tau_i, self.E_e, self.E_i, self.input, int(self.ltc))
+
+
+def lif_coba_step(params: LifParams, V, ge, gi, t_last, spike, dge, dgi, step: int, dt: float):
+  """One neuron-update step in place (torch tensors on the GPU)."""
+  dev = V.device
+  st = _lib.lib().bp_lif_coba_step(ctypes.byref(params.c()), V.shape[0], _lib.ptr(V), _lib.ptr(ge), _lib.ptr(gi),
+                                   _lib.ptr(t_last), _lib.ptr(spike.view(torch.uint8)),
+                                   _lib.ptr(dge) if dge is not None else None,
+                                   _lib.ptr(dgi) if dgi is not None else None, int(step), float(dt),
+                                   _lib.stream_handle(dev))
+  _lib.check(st, "lif_coba_step")
+
+
+class EINetwork:
+  """One E/I COBA network: n neurons, [0, n_exc) excitatory, shared LIF parameters.
+
+  Connectivity is either CSR (``indices``/``indptr`` over all n pre-synaptic rows and n
+  post-synaptic columns: the union of E2E+E2I rows and I2E+I2I rows, homogeneous weights
+  we / wi) or just-in-time (``jitconn=dict(prob=..., seeds=(s_EE, s_EI, s_IE, s_II))``, the
+  four EventJitFPHomoLinear projections of BrainPy, outdim_parallel=True)."""
+
+  def __init__(self, n, n_exc, *, indices=None, indptr=None, we=0.6, wi=6.7, params: Optional[LifParams] = None,
+               jitconn=None, device=None, V0=None):
+    self.n, self.n_exc = int(n), int(n_exc)
+    self.we, self.wi = float(we), float(wi)
+    self.params = params or LifParams()
+    self.device = device or torch.device("cuda", torch.cuda.current_device())
+    self.jitconn = jitconn
+    if jitconn is None:
+      if indices is None or indptr is None:
+        raise ValueError("either CSR (indices, indptr) or jitconn parameters are required")
+      self.indices = indices.to(self.device)
+      self.indptr = indptr.to(self.device)
+    dev = self.device
+    self.V = (torch.as_tensor(V0, dtype=torch.float32, device=dev).clone() if V0 is not None
+              else torch.full((n,), self.params.V_rest, device=dev))
+    self.ge = torch.zeros(n, device=dev)
+    self.gi = torch.zeros(n, device=dev)
+    self.t_last = torch.full((n,), -1e7, device=dev)
+    self.spike = torch.zeros(n, dtype=torch.bool, device=dev)
+    self.t_step = 0
+    self._plan = None
+    self._split = None
+
+  # ---- construction helpers ---------------------------------------------------------
+  @classmethod
+  def fixed_prob(cls, n_exc, n_inh, prob=0.02, we=0.6, wi=6.7, seed=0, params=None, device=None, V0=None):
+    """COBA.py's four FixedProb(prob) projections with fan-out int(post*prob) per group,
+    merged into one n x n CSR (E rows: E targets then I targets; I rows likewise)."""
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    n = n_exc + n_inh
+    blocks = []
+    for g, (rows, seed_off) in enumerate(((n_exc, 0), (n_inh, 2))):
+      i_ee, _ = fixed_prob_csr(rows, n_exc, int(n_exc * prob), seed=seed * 4 + seed_off, device=dev)
+      i_ei, _ = fixed_prob_csr(rows, n_inh, int(n_inh * prob), seed=seed * 4 + seed_off + 1, device=dev)
+      ke, ki = int(n_exc * prob), int(n_inh * prob)
+      row_idx = torch.cat([i_ee.view(rows, ke), i_ei.view(rows, ki) + n_exc], dim=1) if rows else i_ee.view(0, ke + ki)
+      blocks.append(row_idx.reshape(-1))
+    k_row = int(n_exc * prob) + int(n_inh * prob)
+    indices = torch.cat(blocks).to(torch.int32)
+    indptr = (torch.arange(n + 1, device=dev, dtype=torch.int64) * k_row).to(torch.int32)
+    return cls(n, n_exc, indices=indices, indptr=indptr, we=we, wi=wi, params=params, device=dev, V0=V0)
+
+  def state_numpy(self):
+    return {"V": self.V.cpu().numpy(), "ge": self.ge.cpu().numpy(), "gi": self.gi.cpu().numpy(),
+            "t_last": self.t_last.cpu().numpy(), "spike": self.spike.cpu().numpy().astype(np.uint8)}
+
+  # ---- persistent cluster form --------------------------------------------------------
+  def _cluster_plan(self):
+    if self._plan is None:
+      tw = _lib.lib().bp_net_tile_width()
+      self._plan = _event.CSRPlan(self.indices, self.indptr, (self.n, self.n), tile_w=tw, cluster=1)
+      if self._plan.c.n_tiles > _lib.lib().bp_net_max_tiles():
+        raise ValueError(f"network of {self.n} neurons exceeds one cluster ({_lib.lib().bp_net_max_tiles()} tiles)")
+    return self._plan
+
+  def descriptor(self, spike_counts=None, raster=None, v_trace=None, trace_steps=0):
+    plan = self._cluster_plan()
+    rs, toff, idx, w = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    _lib.check(_lib.lib().bp_csr_plan_arrays(ctypes.byref(plan.c), ctypes.byref(rs), ctypes.byref(toff),
+                                             ctypes.byref(idx), ctypes.byref(w)), "csr_plan_arrays")
+    d = _lib.NetDesc()
+    d.n, d.n_exc = self.n, self.n_exc
+    d.tile_w, d.n_tiles = plan.tile_w, plan.c.n_tiles
+    d.row_start, d.tile_off, d.idx = rs, toff, idx
+    d.we, d.wi = self.we, self.wi
+    d.p = self.params.c()
+    d.V, d.ge, d.gi, d.t_last = (self.V.data_ptr(), self.ge.data_ptr(), self.gi.data_ptr(), self.t_last.data_ptr())
+    d.spike = self.spike.data_ptr()
+    d.spike_counts = spike_counts.data_ptr() if spike_counts is not None else None
+    d.raster = raster.data_ptr() if raster is not None else None
+    d.v_trace = v_trace.data_ptr() if v_trace is not None else None
+    d.trace_steps = int(trace_steps)
+    return d
+
+  # ---- per-operator form ------------------------------------------------------------
+  def _csr_split(self):
+    """Views of the merged CSR as an excitatory-row and an inhibitory-row matrix."""
+    if self._split is None:
+      ne = self.n_exc
+      ptr = self.indptr.to(torch.int64)
+      e_end = int(ptr[ne])
+      exc = (self.indices[:e_end], self.indptr[: ne + 1])
+      inh = (self.indices[e_end:], (self.indptr[ne:].to(torch.int64) - e_end).to(self.indptr.dtype))
+      self._split = (exc, inh)
+    return self._split
+
+  def _propagate_ops(self):
+    """Conductance increments of one step from self.spike (per-operator path)."""
+    ne, n = self.n_exc, self.n
+    if not hasattr(self, "_w_t"):
+      self._w_t = (torch.full((1,), self.we, device=self.device), torch.full((1,), self.wi, device=self.device))
+    w_e, w_i = self._w_t
+    if self.jitconn is None:
+      (ie, pe), (ii, pi) = self._csr_split()
+      dge = _event.csrmv(w_e, ie, pe, self.spike[:ne], shape=(ne, n), transpose=True)
+      dgi = _event.csrmv(w_i, ii, pi, self.spike[ne:], shape=(n - ne, n), transpose=True)
+      return dge, dgi
+    p, s = self.jitconn["prob"], self.jitconn["seeds"]
+    ni = n - ne
+    se, si = self.spike[:ne], self.spike[ne:]
+    dge = torch.empty(n, device=self.device)
+    dgi = torch.empty(n, device=self.device)
+    # EventJitFPHomoLinear(num_in, num_out): shape=(num_out, num_in), outdim_parallel=True
+    _jitconn._mv("homo", True, se, self.we, 0.0, p, s[0], (ne, ne), False, True, False, out=dge[:ne])
+    _jitconn._mv("homo", True, se, self.we, 0.0, p, s[1], (ni, ne), False, True, False, out=dge[ne:])
+    _jitconn._mv("homo", True, si, self.wi, 0.0, p, s[2], (ne, ni), False, True, False, out=dgi[:ne])
+    _jitconn._mv("homo", True, si, self.wi, 0.0, p, s[3], (ni, ni), False, True, False, out=dgi[ne:])
+    return dge, dgi
+
+  def step_ops(self, dt, step_dev=None, offset=0):
+    """One step through the per-operator path (propagation calls + neuron kernel)."""
+    dge, dgi = self._propagate_ops()
+    if step_dev is None:
+      lif_coba_step(self.params, self.V, self.ge, self.gi, self.t_last, self.spike, dge, dgi, self.t_step, dt)
+      self.t_step += 1
+      return
+    st = _lib.lib().bp_lif_coba_step_dev(ctypes.byref(self.params.c()), self.n, _lib.ptr(self.V), _lib.ptr(self.ge),
+                                         _lib.ptr(self.gi), _lib.ptr(self.t_last),
+                                         _lib.ptr(self.spike.view(torch.uint8)), _lib.ptr(dge), _lib.ptr(dgi),
+                                         _lib.ptr(step_dev), int(offset), float(dt), _lib.stream_handle(self.device))
+    _lib.check(st, "lif_coba_step_dev")
+
+  def run(self, steps, dt=0.1, method="cluster", spike_counts=None, v_trace_steps=0, graph_steps=0):
+    """Advances `steps` steps.  Returns (spike counts per step [steps] int32, V trace or None).
+    method "cluster": one persistent launch; "ops": per-operator launches, replayed from a
+    CUDA graph of `graph_steps` steps when graph_steps > 0."""
+    counts = spike_counts if spike_counts is not None else torch.zeros(steps, dtype=torch.int32, device=self.device)
+    if method == "cluster":
+      trace = torch.empty((v_trace_steps, self.n), device=self.device) if v_trace_steps else None
+      run_networks([self], steps, dt, spike_counts=[counts], v_traces=[trace] if trace is not None else None,
+                   trace_steps=v_trace_steps)
+      return counts, trace
+    if method != "ops":
+      raise ValueError(f"unknown method {method!r}")
+    if graph_steps:
+      self._run_ops_graph(steps, dt, counts, graph_steps)
+      return counts, None
+    trace = []
+    for s in range(steps):
+      self.step_ops(dt)
+      counts[s] = self.spike.sum()
+      if s < v_trace_steps:
+        trace.append(self.V.clone())
+    return counts, (torch.stack(trace) if trace else None)
+
+  def _run_ops_graph(self, steps, dt, counts, graph_steps):
+    """Per-operator steps replayed from one captured CUDA graph of `graph_steps` steps; the
+    time index comes from device memory so the same graph serves every block of steps."""
+    done = 0
+    if not hasattr(self, "_graph") and steps > 0:
+      self.step_ops(dt)  # warm-up outside capture: plans, workspaces, cached weights
+      counts[0] = self.spike.sum()
+      done = 1
+    if not hasattr(self, "_graph") or self._graph[0] != graph_steps:
+      step_dev = torch.zeros(1, dtype=torch.int32, device=self.device)
+      buf = torch.zeros(graph_steps, dtype=torch.int32, device=self.device)
+      g = torch.cuda.CUDAGraph()
+      torch.cuda.synchronize()
+      with torch.cuda.graph(g):
+        for j in range(graph_steps):
+          self.step_ops(dt, step_dev=step_dev, offset=j)
+          buf[j] = self.spike.sum()
+      self._graph = (graph_steps, g, step_dev, buf)
+    _, g, step_dev, buf = self._graph
+    while steps - done >= graph_steps:
+      step_dev.fill_(self.t_step)
+      g.replay()
+      counts[done:done + graph_steps] = buf
+      self.t_step += graph_steps
+      done += graph_steps
+    while done < steps:
+      self.step_ops(dt)
+      counts[done] = self.spike.sum()
+      done += 1
+    return counts
+
+
+def run_networks(nets, steps, dt=0.1, spike_counts=None, v_traces=None, trace_steps=0, stream=None):
+  """Runs every network for `steps` steps in persistent cluster launches, one launch per
+  cluster size (networks of one size run concurrently, one cluster each)."""
+  if not nets:
+    return
+  dev = nets[0].device
+  groups = {}
+  for k, net in enumerate(nets):
+    d = net.descriptor(spike_counts[k] if spike_counts else None, None,
+                       v_traces[k] if v_traces else None, trace_steps)
+    groups.setdefault(d.n_tiles, []).append((net, d))
+  L = _lib.lib()
+  keep = []
+  for cl, items in sorted(groups.items()):
+    arr = (_lib.NetDesc * len(items))(*[d for _, d in items])
+    buf = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(dev, non_blocking=False)
+    keep.append(buf)
+    st = L.bp_net_run(_lib.ptr(buf), len(items), cl, int(items[0][0].t_step), int(steps), float(dt),
+                      _lib.stream_handle(dev))
+    _lib.check(st, "net_run")
+    for net, _ in items:
+      net.t_step += steps
+  return keep

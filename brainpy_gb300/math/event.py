@@ -71,6 +71,26 @@ class CSRPlan:
     return out
 
 
+  def sparse_t(self, vector, data=None, out=None):
+    """out (n) = A^T vector on this plan (sparse.csrmv, transpose=True)."""
+    dev = self.device
+    m, n = self.shape
+    if vector.shape[0] != m:
+      raise ValueError(f"Shape mismatch, vec ({vector.shape[0]},) @ mat {self.shape}.")
+    if out is None:
+      out = torch.empty(n, dtype=torch.float32, device=dev)
+    L = _lib.lib()
+    w = None
+    if not self.heter:
+      w = data if data is not None else torch.ones(1, dtype=torch.float32, device=dev)
+    ws_bytes = L.bp_event_csrmv_planned_workspace_size(ctypes.byref(self.c))
+    ws = _lib.workspace(ws_bytes, dev)
+    st = L.bp_csrmv_planned(ctypes.byref(self.c), _lib.ptr(w) if w is not None else None, _lib.ptr(vector),
+                            _lib.ptr(out), self.cluster, _lib.ptr(ws), ws_bytes, _lib.stream_handle(dev))
+    _lib.check(st, "csrmv_planned")
+    return out
+
+
 def prepare(indices, indptr, *, shape, data=None, tile_w=None, cluster=4) -> CSRPlan:
   """Builds the tiled plan of a CSR matrix (heterogeneous when `data` has nse entries)."""
   dev = indices.device if isinstance(indices, torch.Tensor) and indices.is_cuda else default_device()

@@ -83,6 +83,52 @@ bp_status bp_event_csrmv(const float* data, int64_t ndata, const void* indices, 
                          size_t workspace_bytes, bp_stream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * sparse.csrmv -- product of a CSR matrix and a dense float32 vector.
+ * Replaces gpu_sparse.cuda_csr_matvec (cuSPARSE; brainpy/_src/math/sparse/_csr_mv.py:197-208),
+ * the brainpylib csrmv_{homo,heter}_{scalar,vector} targets (:257-396) and the Taichi twin
+ * csrmv_taichi (brainpy/_src/math/sparse/_csr_mv_taichi.py:28-287).
+ *   transpose=1: out (n) = A^T vec (vec length m);  transpose=0: out (m) = A vec (vec length n).
+ * Homogeneous weight (ndata == 1): vector values are summed and multiplied by w once.
+ * ------------------------------------------------------------------------- */
+bp_status bp_csrmv(const float* data, int64_t ndata, const void* indices, const void* indptr, bp_itype itype,
+                   int64_t nnz, const float* vec, int64_t m, int64_t n, int32_t transpose, float* out,
+                   bp_stream_t stream);
+
+/* CSR utilities (brainpy/_src/math/sparse/_utils.py:44-114): COO row ids of every stored entry
+ * (same index type as indptr), and the dense (m x n, row-major) matrix with duplicates added. */
+bp_status bp_csr_to_coo(const void* indptr, bp_itype itype, int64_t m, int64_t nnz, void* rows, bp_stream_t stream);
+bp_status bp_csr_to_dense(const float* data, int64_t ndata, const void* indices, const void* indptr, bp_itype itype,
+                          int64_t nnz, int64_t m, int64_t n, float* dense, bp_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * Just-in-time connectivity: y = M v with M regenerated from LFSR88 streams.
+ * Replaces the custom-call families gpu_jit_event_csrmv_{,atomic_}prob_{homo,uniform,normal}_v2*
+ * (brainpy/_src/math/jitconn/_event_matvec.py:198-229, :384-414, :578-608) and
+ * gpu_jit_csrmv_{,atomic_}prob_*_v2* (_matvec.py:341-378, :535-574, :717-760), whose source is
+ * not public; the connectivity follows the reference's in-tree Taichi kernels bit for bit:
+ *   BP_JC_TAICHI_GPU: _event_matvec_taichi.py:96-155 and twins (32 lane streams per owner),
+ *   BP_JC_TAICHI_CPU: _event_matvec_taichi.py:38-85 and twins (one stream per owner).
+ * num_row = output length, num_col = input length (the kernels' own view: for transpose=True
+ * the front-end passes shape[1] outputs and shape[0] inputs).  kind: p0/p1 = weight/unused,
+ * w_low/w_high or mu/sigma.  clen = the connection length int(ceil(1/p))*2-1; seed as uint32.
+ * outdim_parallel=1: pull (deterministic warp sum per output row); 0: push (atomic adds).
+ * Event vectors: only whether an entry is nonzero matters, except that the GPU pull kernels
+ * multiply a float32 event value in (as the reference's GPU kernels do).
+ * ------------------------------------------------------------------------- */
+typedef enum { BP_JC_HOMO = 0, BP_JC_UNIFORM = 1, BP_JC_NORMAL = 2 } bp_jc_kind;
+typedef enum { BP_VEC_EVENT_BOOL = 0, BP_VEC_EVENT_F32 = 1, BP_VEC_DENSE_F32 = 2 } bp_jc_vec;
+typedef enum { BP_JC_TAICHI_GPU = 0, BP_JC_TAICHI_CPU = 1 } bp_jc_variant;
+
+bp_status bp_jitconn_mv(bp_jc_kind kind, bp_jc_vec vec_kind, const void* vec, int64_t num_col, int64_t num_row,
+                        float p0, float p1, int32_t clen, uint32_t seed, int32_t outdim_parallel,
+                        bp_jc_variant variant, float* out, bp_stream_t stream);
+/* Writes M densely (row-major num_row x num_col float32, zeros elsewhere); every connection is
+ * generated once, so this is the exact connectivity and weights the mv kernels use. */
+bp_status bp_jitconn_dense(bp_jc_kind kind, float p0, float p1, int32_t clen, uint32_t seed, int64_t num_row,
+                           int64_t num_col, int32_t outdim_parallel, bp_jc_variant variant, float* dense,
+                           bp_stream_t stream);
+
+/* ---------------------------------------------------------------------------
  * Column-tiled CSR plan (no counterpart in the reference; it plays the role of a
  * cuSPARSE-style analysis step).  A one-time re-layout of a CSR matrix that the tiled
  * event kernels stream: every row's indices regrouped by column tile of tile_w columns,
@@ -112,6 +158,10 @@ bp_status bp_csr_plan_build(const float* data, int64_t ndata, const void* indice
                             bp_itype itype, int64_t nnz, int64_t m, int64_t n, int32_t tile_w, void* mem,
                             size_t bytes, bp_csr_plan* plan_out, bp_stream_t stream);
 
+/* device arrays inside a plan (row_start[m], tile_off[m][n_tiles+1], idx[entries], w or NULL) */
+bp_status bp_csr_plan_arrays(const bp_csr_plan* plan, const uint64_t** row_start, const uint32_t** tile_off,
+                             const uint16_t** idx, const float** w);
+
 /* event.csrmv, transpose=1, on a plan: out (n) = sum of the active rows.  `w_homo` is the
  * homogeneous weight (device pointer to one float) for homogeneous plans and is ignored for
  * heterogeneous ones.  `cluster` = CTAs per column tile (1, 2, 4, 8; 0 = default).
@@ -120,6 +170,11 @@ size_t bp_event_csrmv_planned_workspace_size(const bp_csr_plan* plan);
 bp_status bp_event_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, const void* events, bp_etype etype,
                                  float* out, int32_t cluster, void* workspace, size_t workspace_bytes,
                                  bp_stream_t stream);
+
+/* sparse.csrmv, transpose=1, on a plan: out (n) = A^T vec.  Entries with vec[i] == 0 are
+ * skipped; `w_homo` as for bp_event_csrmv_planned.  Workspace: bp_event_csrmv_planned_workspace_size. */
+bp_status bp_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, const float* vec, float* out,
+                           int32_t cluster, void* workspace, size_t workspace_bytes, bp_stream_t stream);
 
 /* ---------------------------------------------------------------------------
  * event.csrmv with no allocation anywhere (no counterpart in the reference).
@@ -137,6 +192,69 @@ int64_t bp_event_csrmv_noalloc_max_rows(void);
 bp_status bp_event_csrmv_noalloc(const float* data, int64_t ndata, const void* indices, const void* indptr,
                                  bp_itype itype, int64_t nnz, const void* events, bp_etype etype, int64_t m,
                                  int64_t n, int32_t transpose, float* out, bp_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * LIF / Expon / COBA neurons (the consumer of the propagation operators).
+ * No reference counterpart as a kernel: the reference lowers these to XLA elementwise code.
+ * Semantics: LifRefLTC (ltc=1) / LifRef (ltc=0), brainpy/_src/dyn/neurons/lif.py:348-556,
+ * with an excitatory and an inhibitory Expon conductance (abstract_models.py:24-134) feeding
+ * COBA outputs (outputs.py:16-54), exponential Euler (integrators/ode/exponential.py:338-364).
+ * Order within a step: g += dg; g decays; V integrates with the decayed g; refractory;
+ * threshold; reset.  t = float32(step) * dt.  float32, no contraction: results agree bit for
+ * bit with a CPU evaluation in the same operation order.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  float V_rest, V_th, V_reset, tau, tau_ref, R;
+  float tau_e, tau_i, E_e, E_i;
+  float input; /* constant external current (the `inp` passed to the neuron update) */
+  int32_t ltc; /* 1: LifRefLTC (conductance currents inside the derivative); 0: LifRef */
+} bp_lif_params;
+
+/* One step of n neurons: dge/dgi (nullable) are this step's conductance increments. */
+bp_status bp_lif_coba_step(const bp_lif_params* params, int64_t n, float* V, float* ge, float* gi, float* t_last,
+                           uint8_t* spike, const float* dge, const float* dgi, int32_t step, float dt,
+                           bp_stream_t stream);
+
+/* As bp_lif_coba_step with the step index read on the device: step = *step_dev + step_offset
+ * (lets one captured CUDA graph of several steps be replayed at any time). */
+bp_status bp_lif_coba_step_dev(const bp_lif_params* params, int64_t n, float* V, float* ge, float* gi,
+                               float* t_last, uint8_t* spike, const float* dge, const float* dgi,
+                               const int32_t* step_dev, int32_t step_offset, float dt, bp_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * Whole E/I COBA networks in one persistent launch (examples/dynamics_simulation/COBA.py:58-109,
+ * run by DSRunner: brainpy/_src/runners.py:619-665).  No reference counterpart as a kernel.
+ * A network is n neurons ([0, n_exc) excitatory) with one homogeneous-weight CSR matrix over all
+ * n pre-synaptic rows and n post-synaptic columns (E2E+E2I rows, I2E+I2I rows), given as a plan
+ * (bp_csr_plan) whose tiles have tile_w <= 4096 columns; the network runs on a thread-block
+ * cluster of n_tiles CTAs (n_tiles <= 16), every CTA owning one tile of neurons in shared memory.
+ * Per step: the previous step's spikes are propagated (exact integer counts; dg = count * w),
+ * then every neuron is updated.  The descriptor array lives in device memory.
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  int32_t n, n_exc;
+  int32_t tile_w, n_tiles;
+  const uint64_t* row_start; /* plan arrays of the network's CSR (bp_csr_plan, homogeneous) */
+  const uint32_t* tile_off;
+  const uint16_t* idx;
+  float we, wi;
+  bp_lif_params p;
+  float *V, *ge, *gi, *t_last; /* state, length n, updated in place */
+  uint8_t* spike;              /* spikes of the last completed step, length n */
+  int32_t* spike_counts;       /* [steps] spikes per step, accumulated into (nullable) */
+  uint32_t* raster;            /* [steps][ceil(n/32)] spike bits (nullable) */
+  float* v_trace;              /* [trace_steps][n] membrane potential (nullable) */
+  int32_t trace_steps;
+  int32_t reserved;
+} bp_net_desc;
+
+/* largest n_tiles (cluster size) bp_net_run accepts, and the tile width it expects */
+int32_t bp_net_max_tiles(void);
+int32_t bp_net_tile_width(void);
+/* Runs `steps` steps (global step indices step0 .. step0+steps-1) of num_nets networks that all
+ * have n_tiles == cluster, concurrently (one cluster per network). */
+bp_status bp_net_run(const bp_net_desc* descs_device, int32_t num_nets, int32_t cluster, int32_t step0,
+                     int32_t steps, float dt, bp_stream_t stream);
 
 /* ---------------------------------------------------------------------------
  * Kernel timing (benchmark support; no reference counterpart).

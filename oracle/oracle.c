@@ -186,7 +186,8 @@ int64_t orc_jitconn_connections(int32_t kind, float p0, float p1, int32_t clen, 
 }
 
 typedef struct {
-  int32_t vec_kind, outdim_parallel, variant;
+  int32_t vec_kind, outdim_parallel, variant, kind;
+  float p0;
   const void* vec;
   double *out64, *abs64;
 } mv_ctx;
@@ -212,7 +213,12 @@ static void mv_visit(void* ctx, int64_t row, int64_t col, float w) {
   }
   double t = (double)w * f;
   c->out64[row] += t;
-  if (c->abs64) c->abs64[row] += fabs(t);
+  if (c->abs64) {
+    /* normal weights are mu + sigma*z: the rounding of that sum scales with |mu| + |sigma*z|,
+       not with the (possibly cancelled) |w| */
+    double scale = c->kind == 2 ? (fabs((double)c->p0) + fabs((double)w - (double)c->p0)) : fabs((double)w);
+    c->abs64[row] += scale * fabs(f);
+  }
 }
 
 void orc_jitconn_mv(int32_t kind, int32_t vec_kind, const void* vec, int64_t num_row, int64_t num_col,
@@ -229,7 +235,7 @@ void orc_jitconn_mv(int32_t kind, int32_t vec_kind, const void* vec, int64_t num
       else active[j] = ((const float*)vec)[j] != 0.0f;
     }
   }
-  mv_ctx c = {vec_kind, outdim_parallel, variant, vec, out64, abs64};
+  mv_ctx c = {vec_kind, outdim_parallel, variant, kind, p0, vec, out64, abs64};
   jitconn_walk(kind, p0, p1, clen, seed, num_row, num_col, outdim_parallel, variant, active, mv_visit, &c);
   free(active);
 }

@@ -40,7 +40,9 @@ int64_t orc_jitconn_connections(int32_t kind, float p0, float p1, int32_t clen, 
 
 /* y = M v for the jitconn operators.
  * vec_kind: 0 = bool events (uint8), 1 = float32 events, 2 = dense float32 vector (mv_prob_*).
- * Event semantics follow the chosen variant's kernels (see oracle.c). */
+ * Event semantics follow the chosen variant's kernels (see oracle.c).
+ * abs64 is the tolerance scale: sum of |w * v| over the connections, with |w| replaced by
+ * |mu| + |w - mu| for normal weights (the magnitude of the operands of mu + sigma*z). */
 void orc_jitconn_mv(int32_t kind, int32_t vec_kind, const void* vec, int64_t num_row, int64_t num_col,
                     float p0, float p1, int32_t clen, uint32_t seed, int32_t outdim_parallel,
                     int32_t variant, double* out64, double* abs64);

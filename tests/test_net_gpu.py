@@ -1,0 +1,97 @@
+"""E/I COBA networks on the GPU against the oracle.
+
+Event counts are exact integers and the neuron update is evaluated in the same float32
+operation order on both sides, so the simulated trajectories must agree bit for bit:
+membrane potentials of the first 100 steps and spike counts of every step."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dyn(bplib):
+  import brainpy_gb300.dyn as d
+  return d
+
+
+def _oracle_split(net):
+  ind = net.indices.cpu().numpy().astype(np.int32)
+  ptr = net.indptr.cpu().numpy().astype(np.int64)
+  ne = net.n_exc
+  e_end = int(ptr[ne])
+  exc_ptr = ptr[: ne + 1].astype(np.int32)
+  inh_ptr = (ptr[ne:] - e_end).astype(np.int32)
+  return exc_ptr, np.ascontiguousarray(ind[:e_end]), inh_ptr, np.ascontiguousarray(ind[e_end:])
+
+
+def _oracle_run(orc, net, state, steps, trace_steps=0, step0=0):
+  p = net.params
+  op = orc.lif_params(p.V_rest, p.V_th, p.V_reset, p.tau, p.tau_ref, p.R, p.tau_e, p.tau_i, p.E_e, p.E_i, p.input,
+                      p.ltc)
+  ep, ei, ip, ii = _oracle_split(net)
+  return orc.coba_net_run(op, net.n, net.n_exc, ep, ei, np.float32(net.we), ip, ii, np.float32(net.wi), state,
+                          step0, steps, np.float32(0.1), count_mode=True, trace_steps=trace_steps)
+
+
+def _v0(n, seed=3):
+  return np.random.default_rng(seed).normal(-55.0, 5.0, n).astype(np.float32)
+
+
+@pytest.mark.parametrize("ltc", [True, False])
+def test_coba_4000_bit_exact(dyn, orc, ltc):
+  """The COBA example network (3200 E + 800 I, 2 % FixedProb, we 0.6, wi 6.7)."""
+  V0 = _v0(4000)
+  net = dyn.EINetwork.fixed_prob(3200, 800, prob=0.02, seed=1, params=dyn.LifParams(ltc=ltc), V0=V0)
+  state = net.state_numpy()
+  counts, trace = net.run(1000, method="cluster", v_trace_steps=100)
+  rc, rtrace = _oracle_run(orc, net, state, 1000, trace_steps=100)
+  np.testing.assert_array_equal(trace.cpu().numpy(), rtrace)  # V within 0 mV over the first 100 steps
+  np.testing.assert_array_equal(counts.cpu().numpy(), rc)
+  got = net.state_numpy()
+  for k in ("V", "ge", "gi", "t_last", "spike"):
+    np.testing.assert_array_equal(got[k], state[k], err_msg=k)
+  assert rc.sum() > 1000  # the network is active
+
+
+def test_ops_path_and_graph_match_cluster(dyn):
+  V0 = _v0(4000, seed=4)
+  a = dyn.EINetwork.fixed_prob(3200, 800, seed=2, V0=V0)
+  b = dyn.EINetwork(a.n, a.n_exc, indices=a.indices, indptr=a.indptr, V0=V0)
+  c = dyn.EINetwork(a.n, a.n_exc, indices=a.indices, indptr=a.indptr, V0=V0)
+  ca, _ = a.run(300, method="cluster")
+  cb, _ = b.run(300, method="ops")
+  cc, _ = c.run(300, method="ops", graph_steps=50)
+  assert torch.equal(ca, cb) and torch.equal(ca, cc)
+  assert torch.equal(a.V, b.V) and torch.equal(a.V, c.V)
+
+
+def test_many_networks_of_uneven_sizes(dyn, orc):
+  """Networks needing 1, 2, 4 and 16 CTAs run concurrently in one call per cluster size."""
+  rng = np.random.default_rng(7)
+  sizes = [1000, 2500, 6000, 9000, 15000, 62000]
+  nets, states = [], []
+  for k, n in enumerate(sizes):
+    ne = int(0.8 * n)
+    net = dyn.EINetwork.fixed_prob(ne, n - ne, prob=0.02, we=float(rng.uniform(0.3, 1.0)),
+                                   wi=float(rng.uniform(3, 10)), seed=10 + k, V0=_v0(n, seed=20 + k))
+    nets.append(net)
+    states.append(net.state_numpy())
+  counts = [torch.zeros(60, dtype=torch.int32, device="cuda") for _ in nets]
+  dyn.run_networks(nets, 60, spike_counts=counts)
+  for net, st, cnt in zip(nets, states, counts):
+    rc, _ = _oracle_run(orc, net, st, 60)
+    np.testing.assert_array_equal(cnt.cpu().numpy(), rc)
+    np.testing.assert_array_equal(net.V.cpu().numpy(), st["V"])
+
+
+def test_continue_across_calls(dyn):
+  """Two runs of 40 steps equal one run of 80 (state, spikes and time index carried over)."""
+  V0 = _v0(4000, seed=5)
+  a = dyn.EINetwork.fixed_prob(3200, 800, seed=3, V0=V0)
+  b = dyn.EINetwork(a.n, a.n_exc, indices=a.indices, indptr=a.indptr, V0=V0)
+  c1, _ = a.run(40)
+  c2, _ = a.run(40)
+  cb, _ = b.run(80)
+  assert torch.equal(torch.cat([c1, c2]), cb) and torch.equal(a.V, b.V)

@@ -42,6 +42,13 @@ def parse():
   ap.add_argument("--weights", default="homo", choices=["homo", "heter"])
   ap.add_argument("--no-cpu-baseline", action="store_true")
   ap.add_argument("--cpu-seconds", type=float, default=12.0)
+  ap.add_argument("--workload", default="event_csrmv",
+                  choices=["event_csrmv", "coba", "batched", "jitconn_net", "serve"],
+                  help="event_csrmv (headline); coba: the 4000-neuron COBA example; batched: 256 uneven "
+                       "networks in persistent cluster launches vs the plain per-network path; jitconn_net: "
+                       "4M-neuron just-in-time network; serve: continuous-batching serving loop")
+  ap.add_argument("--nets", type=int, default=256)
+  ap.add_argument("--sim-steps", type=int, default=0, help="override the workload's number of steps")
   return ap.parse_args()
 
 
@@ -180,6 +187,12 @@ def run_reference(args):
 
 def main():
   args = parse()
+  if args.workload != "event_csrmv":
+    fn = {"coba": bench_coba, "batched": bench_batched, "jitconn_net": bench_jitconn_net, "serve": bench_serve}
+    line = fn[args.workload](args)
+    if line is not None:
+      print(json.dumps(line))
+    return
   if args.impl == "reference":
     run_reference(args)
     return
@@ -286,6 +299,165 @@ def main():
     print(json.dumps(line))
   if ws > 1:
     torch.distributed.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------------------
+# network workloads
+# ---------------------------------------------------------------------------------------
+def _cuda_time(fn):
+  torch.cuda.synchronize()
+  e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  e0.record()
+  out = fn()
+  e1.record()
+  e1.synchronize()
+  return e0.elapsed_time(e1) * 1e-3, out
+
+
+def bench_coba(args):
+  """The COBA example: 3200 E + 800 I LifRefLTC, 2 % FixedProb, 10000 steps of 0.1 ms."""
+  import oracle
+  from brainpy_gb300 import dyn
+  steps = args.sim_steps or 10000
+  V0 = np.random.default_rng(3).normal(-55.0, 5.0, 4000).astype(np.float32)
+  net = dyn.EINetwork.fixed_prob(3200, 800, prob=0.02, seed=0, V0=V0)
+  net.run(100)  # warm-up: plan build, module load
+  net2 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=V0)
+  clocks = ClockSampler(torch.cuda.current_device())
+  counts = torch.zeros(steps, dtype=torch.int32, device="cuda")
+  t_cluster, _ = _cuda_time(lambda: net2.run(steps, spike_counts=counts))
+  clk = clocks.stop()
+  n_spk = int(counts.sum())
+  fan = 64 + 16
+  # per-operator path, host loop and CUDA-graph replay, on a bounded number of steps
+  k_ops = min(steps, 1000)
+  net3 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=V0)
+  net3.run(5, method="ops")
+  t_ops, _ = _cuda_time(lambda: net3.run(k_ops, method="ops"))
+  net4 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=V0)
+  net4.run(60, method="ops", graph_steps=50)
+  t_graph, _ = _cuda_time(lambda: net4.run(k_ops, method="ops", graph_steps=50))
+  # e2e: host V0 in, spike counts out, whole run through the public API
+  host_v0 = torch.from_numpy(V0).pin_memory()
+  def e2e():
+    n5 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=host_v0)
+    c, _ = n5.run(steps)
+    return c.cpu()
+  t_e2e, _ = _cuda_time(e2e)
+  # CPU: the oracle's restatement of the reference step, single thread, bounded sample
+  st = net.state_numpy()
+  st = {k: v.copy() for k, v in net2.state_numpy().items()}
+  st["V"][:] = V0
+  st["ge"][:] = 0
+  st["gi"][:] = 0
+  st["t_last"][:] = -1e7
+  st["spike"][:] = 0
+  ind = net.indices.cpu().numpy()
+  ptr = net.indptr.cpu().numpy().astype(np.int64)
+  e_end = int(ptr[3200])
+  op = oracle.lif_params()
+  k_cpu = min(steps, 2000)
+  t0 = time.perf_counter()
+  oracle.coba_net_run(op, 4000, 3200, ptr[:3201].astype(np.int32), np.ascontiguousarray(ind[:e_end]),
+                      np.float32(0.6), (ptr[3200:] - e_end).astype(np.int32), np.ascontiguousarray(ind[e_end:]),
+                      np.float32(6.7), st, 0, k_cpu, np.float32(0.1))
+  t_cpu = time.perf_counter() - t0
+  return {"metric": "network-steps/s (COBA E/I 4000 neurons, dt 0.1 ms)", "value": steps / t_cluster,
+          "unit": "steps/s", "n_gpus": 1, "steps": steps, "warmup": 100, "ms_per_step": t_cluster / steps * 1e3,
+          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+          "config": {"workload": "COBA 3200E+800I FixedProb(0.02) LifRefLTC, 10000 steps", "path": "persistent cluster"},
+          "synaptic_events_per_s": n_spk * fan / t_cluster, "firing_rate_hz": n_spk / 4000 / (steps * 1e-4),
+          "per_op_path_steps_per_s": k_ops / t_ops, "per_op_graph_steps_per_s": k_ops / t_graph,
+          "e2e": {"value": steps / t_e2e, "unit": "steps/s", "h2d_bytes_per_step": 4000 * 4 / steps,
+                  "d2h_bytes_per_step": 4},
+          "cpu_baseline": {"value": k_cpu / t_cpu, "unit": "steps/s", "cores": 1, "kind": "port",
+                           "sample": f"{k_cpu} steps of the oracle's float32 restatement (oracle.c orc_coba_net_run)"},
+          "clocks": clk, "gpu_launches": 1}
+
+
+def bench_batched(args):
+  """256 independent COBA networks, N ~ logU[1k, 64k], we ~ U[0.3, 1], wi ~ U[3, 10], 5000 steps,
+  all in persistent cluster launches, against the plain per-network path (one network at a
+  time, one kernel per operator per step, host loop)."""
+  from brainpy_gb300 import dyn
+  steps = args.sim_steps or 5000
+  rng = np.random.default_rng(11)
+  sizes = np.exp(rng.uniform(np.log(1000), np.log(64000), args.nets)).astype(int)
+  nets = []
+  for k, n in enumerate(sizes):
+    ne = int(0.8 * n)
+    nets.append(dyn.EINetwork.fixed_prob(ne, n - ne, prob=0.02, we=float(rng.uniform(0.3, 1.0)),
+                                         wi=float(rng.uniform(3.0, 10.0)), seed=100 + k,
+                                         V0=rng.normal(-55.0, 5.0, n).astype(np.float32)))
+  init = [(x.V.clone(), x.ge.clone(), x.gi.clone(), x.t_last.clone(), x.spike.clone()) for x in nets]
+  for x in nets:
+    x._cluster_plan()
+  k_plain = 20
+  counts = [torch.zeros(steps, dtype=torch.int32, device="cuda") for _ in nets]
+  clocks = ClockSampler(torch.cuda.current_device())
+  t_batch, _ = _cuda_time(lambda: dyn.run_networks(nets, steps, spike_counts=counts))
+  clk = clocks.stop()
+  fan = np.array([int(0.8 * n * 0.02) + int((n - int(0.8 * n)) * 0.02) for n in sizes])
+  n_spk = np.array([int(c.sum()) for c in counts])
+  # plain path: every network from its initial state, k_plain steps each, one after another
+  # (warmed up first so that plans and workspaces exist, then reset to the initial state)
+  plain = []
+  for x, st in zip(nets, init):
+    y = dyn.EINetwork(x.n, x.n_exc, indices=x.indices, indptr=x.indptr, we=x.we, wi=x.wi, V0=st[0])
+    y.run(1, method="ops")
+    y.reset_state(*st)
+    plain.append(y)
+  pc = []
+  def run_plain():
+    for y in plain:
+      c, _ = y.run(k_plain, method="ops")
+      pc.append(c)
+  t_plain, _ = _cuda_time(run_plain)
+  same = all(torch.equal(c[:k_plain], p) for c, p in zip(counts, pc))
+  v_batch = len(nets) * steps / t_batch
+  v_plain = len(nets) * k_plain / t_plain
+  return {"metric": "network-steps/s (256 uneven COBA networks, batched)", "value": v_batch, "unit": "network-steps/s",
+          "n_gpus": 1, "steps": steps, "warmup": 0, "ms_per_step": t_batch / steps * 1e3, "higher_is_better": True,
+          "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+          "config": {"workload": f"{len(nets)} networks N~logU[1k,64k], 2% FixedProb, {steps} steps",
+                     "neurons_total": int(sizes.sum())},
+          "synaptic_events_per_s": float((n_spk * fan).sum()) / t_batch,
+          "plain_per_network_path": {"value": v_plain, "unit": "network-steps/s",
+                                     "sample": f"all {len(nets)} networks x {k_plain} steps, per-operator kernels, host loop"},
+          "speedup_vs_plain": v_batch / v_plain,
+          "accuracy": "bit-identical spike counts over the first %d steps of every network: %s" % (k_plain, same),
+          "clocks": clk, "gpu_launches": len({x.descriptor().n_tiles for x in nets})}
+
+
+def bench_jitconn_net(args):
+  """4M-neuron E/I COBA network (80/20), fan-in 1000 regenerated by event_mv_prob_homo
+  (no stored matrix), per-operator path replayed from CUDA graphs of 50 steps."""
+  from brainpy_gb300 import dyn
+  steps = args.sim_steps or 1000
+  n = 4_000_000
+  ne = int(0.8 * n)
+  p = 1000 / n
+  V0 = np.random.default_rng(5).normal(-55.0, 5.0, n).astype(np.float32)
+  # COBA's weights scaled by 80/1000 keep the example's total synaptic drive at fan-in 1000
+  net = dyn.EINetwork(n, ne, jitconn=dict(prob=p, seeds=(11, 12, 13, 14)), we=0.6 * 0.08, wi=6.7 * 0.08, V0=V0)
+  counts = torch.zeros(steps + 60, dtype=torch.int32, device="cuda")
+  net.run(60, method="ops", graph_steps=50, spike_counts=counts[:60])
+  clocks = ClockSampler(torch.cuda.current_device())
+  t, _ = _cuda_time(lambda: net.run(steps, method="ops", graph_steps=50, spike_counts=counts[60:]))
+  clk = clocks.stop()
+  n_spk = int(counts[60:].sum())
+  return {"metric": "network-steps/s (4M-neuron jitconn E/I network)", "value": steps / t, "unit": "steps/s",
+          "n_gpus": 1, "steps": steps, "warmup": 60, "ms_per_step": t / steps * 1e3, "higher_is_better": True,
+          "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+          "config": {"workload": "4M neurons 80/20, fan-in 1000 via event_mv_prob_homo (outdim_parallel=True), "
+                                 "we=0.048 wi=0.536 (COBA weights x 80/1000)"},
+          "synaptic_events_per_s": n_spk * 1000 / t, "connections_generated_per_s": 4e9 / (t / steps),
+          "firing_rate_hz": n_spk / n / (steps * 1e-4), "clocks": clk}
+
+
+def bench_serve(args):
+  from brainpy_gb300 import serve
+  return serve.bench(args)
 
 
 def launches_per_step(args):

@@ -107,6 +107,15 @@ class EINetwork:
     indptr = (torch.arange(n + 1, device=dev, dtype=torch.int64) * k_row).to(torch.int32)
     return cls(n, n_exc, indices=indices, indptr=indptr, we=we, wi=wi, params=params, device=dev, V0=V0)
 
+  def reset_state(self, V, ge, gi, t_last, spike, t_step=0):
+    """Overwrites the state (tensors of length n) and the time index."""
+    self.V.copy_(V)
+    self.ge.copy_(ge)
+    self.gi.copy_(gi)
+    self.t_last.copy_(t_last)
+    self.spike.copy_(spike)
+    self.t_step = int(t_step)
+
   def state_numpy(self):
     return {"V": self.V.cpu().numpy(), "ge": self.ge.cpu().numpy(), "gi": self.gi.cpu().numpy(),
             "t_last": self.t_last.cpu().numpy(), "spike": self.spike.cpu().numpy().astype(np.uint8)}

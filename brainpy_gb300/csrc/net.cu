@@ -92,7 +92,8 @@ __global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_ne
   }
   cluster.sync();
 
-  for (int s = 0; s < steps; ++s) {
+  const int my_steps = d.step_limit > 0 ? min(steps, d.step_limit) : steps;
+  for (int s = 0; s < my_steps; ++s) {
     const int cur = s & 1, nxt = cur ^ 1;
     // ---- 1. propagate the previous step's spikes into this tile's counters
     int pre[kNetMaxTiles + 1];
@@ -135,7 +136,7 @@ __global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_ne
     }
     __syncthreads();
     // ---- 2. neuron update
-    const float t = __fmul_rn((float)(step0 + s), dt);
+    const float t = __fmul_rn((float)(step0 + d.step0 + s), dt);
     if (tid == 0) S.cnt[nxt] = 0;
     __syncthreads();
     for (int k0 = 0; k0 < tw; k0 += blockDim.x) {
@@ -168,7 +169,7 @@ __global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_ne
   }
 
   // write back state and the last step's spikes
-  const int last = steps & 1;
+  const int last = my_steps & 1;
   for (int k = tid; k < nloc; k += blockDim.x) {
     d.V[base + k] = S.V[k];
     d.ge[base + k] = S.ge[k];

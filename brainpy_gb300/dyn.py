@@ -129,7 +129,7 @@ class EINetwork:
         raise ValueError(f"network of {self.n} neurons exceeds one cluster ({_lib.lib().bp_net_max_tiles()} tiles)")
     return self._plan
 
-  def descriptor(self, spike_counts=None, raster=None, v_trace=None, trace_steps=0):
+  def descriptor(self, spike_counts=None, raster=None, v_trace=None, trace_steps=0, step_limit=0):
     plan = self._cluster_plan()
     rs, toff, idx, w = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
     _lib.check(_lib.lib().bp_csr_plan_arrays(ctypes.byref(plan.c), ctypes.byref(rs), ctypes.byref(toff),
@@ -146,6 +146,8 @@ class EINetwork:
     d.raster = raster.data_ptr() if raster is not None else None
     d.v_trace = v_trace.data_ptr() if v_trace is not None else None
     d.trace_steps = int(trace_steps)
+    d.step_limit = int(step_limit)
+    d.step0 = int(self.t_step)
     return d
 
   # ---- per-operator form ------------------------------------------------------------
@@ -172,15 +174,16 @@ class EINetwork:
       dgi = _event.csrmv(w_i, ii, pi, self.spike[ne:], shape=(n - ne, n), transpose=True)
       return dge, dgi
     p, s = self.jitconn["prob"], self.jitconn["seeds"]
+    odp = bool(self.jitconn.get("outdim_parallel", True))
     ni = n - ne
     se, si = self.spike[:ne], self.spike[ne:]
     dge = torch.empty(n, device=self.device)
     dgi = torch.empty(n, device=self.device)
-    # EventJitFPHomoLinear(num_in, num_out): shape=(num_out, num_in), outdim_parallel=True
-    _jitconn._mv("homo", True, se, self.we, 0.0, p, s[0], (ne, ne), False, True, False, out=dge[:ne])
-    _jitconn._mv("homo", True, se, self.we, 0.0, p, s[1], (ni, ne), False, True, False, out=dge[ne:])
-    _jitconn._mv("homo", True, si, self.wi, 0.0, p, s[2], (ne, ni), False, True, False, out=dgi[:ne])
-    _jitconn._mv("homo", True, si, self.wi, 0.0, p, s[3], (ni, ni), False, True, False, out=dgi[ne:])
+    # EventJitFPHomoLinear(num_in, num_out, atomic=not odp): shape=(num_out, num_in)
+    _jitconn._mv("homo", True, se, self.we, 0.0, p, s[0], (ne, ne), False, odp, False, out=dge[:ne])
+    _jitconn._mv("homo", True, se, self.we, 0.0, p, s[1], (ni, ne), False, odp, False, out=dge[ne:])
+    _jitconn._mv("homo", True, si, self.wi, 0.0, p, s[2], (ne, ni), False, odp, False, out=dgi[:ne])
+    _jitconn._mv("homo", True, si, self.wi, 0.0, p, s[3], (ni, ni), False, odp, False, out=dgi[ne:])
     return dge, dgi
 
   def step_ops(self, dt, step_dev=None, offset=0):
@@ -251,26 +254,27 @@ class EINetwork:
     return counts
 
 
-def run_networks(nets, steps, dt=0.1, spike_counts=None, v_traces=None, trace_steps=0, stream=None):
-  """Runs every network for `steps` steps in persistent cluster launches, one launch per
-  cluster size (networks of one size run concurrently, one cluster each)."""
+def run_networks(nets, steps, dt=0.1, spike_counts=None, v_traces=None, trace_steps=0, step_limits=None):
+  """Runs every network for `steps` steps (or its own step limit) in persistent cluster
+  launches, one launch per cluster size: networks of one size run concurrently, one cluster
+  each, each at its own time index."""
   if not nets:
     return
   dev = nets[0].device
   groups = {}
   for k, net in enumerate(nets):
+    lim = int(step_limits[k]) if step_limits is not None else 0
     d = net.descriptor(spike_counts[k] if spike_counts else None, None,
-                       v_traces[k] if v_traces else None, trace_steps)
-    groups.setdefault(d.n_tiles, []).append((net, d))
+                       v_traces[k] if v_traces else None, trace_steps, lim)
+    groups.setdefault(d.n_tiles, []).append((net, d, lim))
   L = _lib.lib()
   keep = []
   for cl, items in sorted(groups.items()):
-    arr = (_lib.NetDesc * len(items))(*[d for _, d in items])
+    arr = (_lib.NetDesc * len(items))(*[d for _, d, _ in items])
     buf = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(dev, non_blocking=False)
     keep.append(buf)
-    st = L.bp_net_run(_lib.ptr(buf), len(items), cl, int(items[0][0].t_step), int(steps), float(dt),
-                      _lib.stream_handle(dev))
+    st = L.bp_net_run(_lib.ptr(buf), len(items), cl, 0, int(steps), float(dt), _lib.stream_handle(dev))
     _lib.check(st, "net_run")
-    for net, _ in items:
-      net.t_step += steps
+    for net, _, lim in items:
+      net.t_step += min(steps, lim) if lim > 0 else steps
   return keep

@@ -245,6 +245,8 @@ typedef struct {
   uint32_t* raster;            /* [steps][ceil(n/32)] spike bits (nullable) */
   float* v_trace;              /* [trace_steps][n] membrane potential (nullable) */
   int32_t trace_steps;
+  int32_t step_limit;          /* > 0: this network stops after step_limit of the launch's steps */
+  int32_t step0;               /* time index of this network's first step (added to the launch's step0) */
   int32_t reserved;
 } bp_net_desc;
 

@@ -17,6 +17,8 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 
 #include "common.cuh"
 #include "compact.cuh"
@@ -184,7 +186,7 @@ struct TiledArgs {
 // and the descriptors of slice k+W are in flight while slice k is processed.  Inside a slice,
 // groups of G lanes take one segment each (lane gl loads 8-byte chunk gl, 4 uint16 indices)
 // and G segments are loaded back to back before any shared-memory atomic is issued.
-template <int MODE>
+template <int MODE, int G, int RND>
 __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArgs a) {
   constexpr bool HAS_W = (MODE == kWeight || MODE == kWRow);
   constexpr bool HAS_X = (MODE == kRowVal || MODE == kWRow);
@@ -289,22 +291,54 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArg
         blk3 = block_of(min(((k + 2 * nwarps) << 5) + lane, max(total - 1, 0)));
         row2 = fetch_row(k + 2 * nwarps, blk3);
       }
-      // this lane's segment: chunks [0, cn) at entry cst; U chunk loads before the atomics
-      constexpr int U = HAS_W ? 4 : 8;
-      for (uint32_t c0 = 0; __any_sync(0xffffffffu, c0 < cn); c0 += U) {
-        uint2 vv[U];
-        float4 wv[U];
+      // Groups of G lanes share a segment: group grp takes the segments of lanes
+      // grp, grp + 32/G, ...; lane gl of the group loads chunks gl, gl + G, ... (RND rounds),
+      // so one warp-wide load touches 32/G segments with G consecutive chunks each.  UB
+      // segments are loaded before any of their atomics are issued.
+      {
+        constexpr int NG = 32 / G;
+        constexpr int UBMAX = (HAS_W ? 4 : 8) / RND > 0 ? (HAS_W ? 4 : 8) / RND : 1;
+        constexpr int UB = UBMAX > G ? G : UBMAX;
+        const int grp = lane / G, gl = lane % G;
+#pragma unroll 1
+        for (int u0 = 0; u0 < G; u0 += UB) {
+          uint2 vv[UB][RND];
+          float4 wv[UB][RND];
+          uint32_t st[UB], ln[UB];
+          float xs[UB];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          if (c0 + u < cn) {
-            const uint32_t e = cst + 4u * (c0 + u);
-            vv[u] = ld_stream_u2(a.idx + e);
-            if (HAS_W) wv[u] = ld_stream_f4(a.w + e);
+          for (int u = 0; u < UB; ++u) {
+            const int j = grp + (u0 + u) * NG;
+            st[u] = __shfl_sync(0xffffffffu, cst, j);
+            ln[u] = __shfl_sync(0xffffffffu, cn, j);
+            xs[u] = HAS_X ? __shfl_sync(0xffffffffu, cxv, j) : 0.0f;
+#pragma unroll
+            for (int r = 0; r < RND; ++r) {
+              const uint32_t c = gl + r * G;
+              if (c < ln[u]) {
+                const uint32_t e = st[u] + 4u * c;
+                vv[u][r] = ld_stream_u2(a.idx + e);
+                if (HAS_W) wv[u][r] = ld_stream_f4(a.w + e);
+              }
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < UB; ++u)
+#pragma unroll
+            for (int r = 0; r < RND; ++r)
+              if (gl + r * G < ln[u])
+                accumulate4<MODE>(acc, vv[u][r], HAS_W ? wv[u][r] : make_float4(0, 0, 0, 0), xs[u], a.tile_w);
+          // chunks beyond RND*G (long segments): rare, plain loop
+#pragma unroll
+          for (int u = 0; u < UB; ++u) {
+            for (uint32_t c = gl + RND * G; c < ln[u]; c += G) {
+              const uint32_t e = st[u] + 4u * c;
+              const uint2 x = ld_stream_u2(a.idx + e);
+              const float4 y = HAS_W ? ld_stream_f4(a.w + e) : make_float4(0, 0, 0, 0);
+              accumulate4<MODE>(acc, x, y, xs[u], a.tile_w);
+            }
           }
         }
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-          if (c0 + u < cn) accumulate4<MODE>(acc, vv[u], HAS_W ? wv[u] : make_float4(0, 0, 0, 0), cxv, a.tile_w);
       }
       cst = nst;
       cn = nn;
@@ -375,9 +409,9 @@ static int acc_words_for(int tile_w, int R) {
   return (tile_w + q - 1) / q * q;
 }
 
-template <int MODE>
-static bp_status launch_tiled(const TiledArgs& a, int R, cudaStream_t st) {
-  auto kfn = ecsr_t_tiled_kernel<MODE>;
+template <int MODE, int G, int RND>
+static bp_status launch_tiled_g(const TiledArgs& a, int R, cudaStream_t st) {
+  auto kfn = ecsr_t_tiled_kernel<MODE, G, RND>;
   const size_t smem = tiled_smem_bytes(a.acc_words);
   static thread_local size_t configured[64] = {0};
   int dev = 0;
@@ -406,6 +440,39 @@ static bp_status launch_tiled(const TiledArgs& a, int R, cudaStream_t st) {
   return BP_OK;
 }
 
+// (lanes per segment, chunk rounds) from the mean segment length in 8-byte chunks; the
+// environment variable BPGPU_TILED_GROUP=G,RND overrides (tuning).
+static void choose_group(double chunks, int& G, int& RND) {
+  if (chunks <= 1.5) { G = 1; RND = 2; }
+  else if (chunks <= 4.5) { G = 2; RND = 2; }
+  else if (chunks <= 10.0) { G = 4; RND = 2; }
+  else if (chunks <= 14.0) { G = 4; RND = 3; }
+  else { G = 8; RND = 2; }
+  static int env_g = -1, env_r = -1;
+  if (env_g < 0) {
+    env_g = 0;
+    const char* e = getenv("BPGPU_TILED_GROUP");
+    if (e) sscanf(e, "%d,%d", &env_g, &env_r);
+  }
+  if (env_g > 0) {
+    G = env_g;
+    RND = env_r > 0 ? env_r : 2;
+  }
+}
+
+template <int MODE>
+static bp_status launch_tiled(const TiledArgs& a, int R, double chunks, cudaStream_t st) {
+  int G, RND;
+  choose_group(chunks, G, RND);
+  if (G == 1) return launch_tiled_g<MODE, 1, 2>(a, R, st);
+  if (G == 2) return launch_tiled_g<MODE, 2, 2>(a, R, st);
+  if (G == 4 && RND == 2) return launch_tiled_g<MODE, 4, 2>(a, R, st);
+  if (G == 4) return launch_tiled_g<MODE, 4, 3>(a, R, st);
+  if (G == 8 && RND == 1) return launch_tiled_g<MODE, 8, 1>(a, R, st);
+  if (G == 8) return launch_tiled_g<MODE, 8, 2>(a, R, st);
+  return launch_tiled_g<MODE, 16, 1>(a, R, st);
+}
+
 template <int ET>
 static bp_status launch_compact_blocked(const void* events, int64_t m, int32_t* lists, int32_t* counts,
                                         cudaStream_t st) {
@@ -425,7 +492,7 @@ static bp_status compact_blocked(const void* events, bp_etype et, int64_t m, int
 }
 
 static int max_active_clusters(int R, size_t smem) {
-  auto kfn = ecsr_t_tiled_kernel<kCount>;
+  auto kfn = ecsr_t_tiled_kernel<kCount, 4, 3>;
   if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
   cudaFuncSetAttribute(kfn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   cudaLaunchConfig_t cfg = {};
@@ -616,7 +683,8 @@ bp_status bp_event_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, c
   a.nb = nb;
   a.acc_words = acc_words;
   a.vec_out = ((reinterpret_cast<uintptr_t>(out) & 15u) == 0) ? 1 : 0;
-  s = homo ? launch_tiled<kCount>(a, cluster, st) : launch_tiled<kWeight>(a, cluster, st);
+  const double chunks = ((double)plan->nnz / (double)m / (double)plan->n_tiles + 1.5) / 4.0;
+  s = homo ? launch_tiled<kCount>(a, cluster, chunks, st) : launch_tiled<kWeight>(a, cluster, chunks, st);
   return s;
 }
 
@@ -674,7 +742,8 @@ bp_status bp_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, const f
   a.nb = nb;
   a.acc_words = acc_words;
   a.vec_out = ((reinterpret_cast<uintptr_t>(out) & 15u) == 0) ? 1 : 0;
-  return homo ? launch_tiled<kRowVal>(a, cluster, st) : launch_tiled<kWRow>(a, cluster, st);
+  const double chunks = ((double)plan->nnz / (double)m / (double)plan->n_tiles + 1.5) / 4.0;
+  return homo ? launch_tiled<kRowVal>(a, cluster, chunks, st) : launch_tiled<kWRow>(a, cluster, chunks, st);
 }
 
 }  // extern "C"

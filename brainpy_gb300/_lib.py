@@ -51,8 +51,7 @@ SIGNATURES = {
     "bp_event_csrmv_planned_workspace_size": (_c_size, [_c_ptr]),
     "bp_event_csrmv_planned": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_i32, _c_ptr, _c_i32, _c_ptr, _c_size, _c_ptr]),
     "bp_csrmv_planned": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i32, _c_ptr, _c_size, _c_ptr]),
-    "bp_csr_plan_arrays": (_c_i32, [_c_ptr, ctypes.POINTER(_c_ptr), ctypes.POINTER(_c_ptr), ctypes.POINTER(_c_ptr),
-                                    ctypes.POINTER(_c_ptr)]),
+    "bp_csr_plan_arrays": (_c_i32, [_c_ptr, ctypes.POINTER(_c_ptr), ctypes.POINTER(_c_ptr), ctypes.POINTER(_c_ptr)]),
     "bp_lif_coba_step": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i32,
                                   _c_f32, _c_ptr]),
     "bp_lif_coba_step_dev": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr,
@@ -85,7 +84,7 @@ class LifParams(ctypes.Structure):
 class NetDesc(ctypes.Structure):
   """Mirror of bp_net_desc (include/bpgpu.h)."""
   _fields_ = [("n", _c_i32), ("n_exc", _c_i32), ("tile_w", _c_i32), ("n_tiles", _c_i32),
-              ("row_start", _c_ptr), ("tile_off", _c_ptr), ("idx", _c_ptr), ("we", _c_f32), ("wi", _c_f32),
+              ("seg_off", _c_ptr), ("idx", _c_ptr), ("we", _c_f32), ("wi", _c_f32),
               ("p", LifParams), ("V", _c_ptr), ("ge", _c_ptr), ("gi", _c_ptr), ("t_last", _c_ptr),
               ("spike", _c_ptr), ("spike_counts", _c_ptr), ("raster", _c_ptr), ("v_trace", _c_ptr),
               ("trace_steps", _c_i32), ("step_limit", _c_i32), ("step0", _c_i32), ("reserved", _c_i32)]

@@ -6,10 +6,11 @@
 //      `counts` -- no atomics, nothing to reset between calls.
 //   2. ecsr_t_tiled_kernel: a thread-block cluster of R CTAs owns one tile of tile_w output
 //      columns.  CTA `rank` takes 1/R of the compaction blocks; for each active row it loads
-//      the row's segment for its tile (tile-local uint16 indices in 8-byte chunks) and adds
+//      the row's segment for its tile (16-byte chunks of 8 tile-local uint16 indices) and adds
 //      into a shared-memory accumulator (uint32 counts for a homogeneous weight, float32
-//      otherwise).  At the end the R accumulators of the cluster are summed through
-//      distributed shared memory and every output column is written exactly once.
+//      otherwise), with the next rows' segments prefetched into L2.  At the end the R
+//      accumulators of the cluster are summed through distributed shared memory and every
+//      output column is written exactly once.
 //
 // The random scatter thus stays on-chip (shared-memory atomics), HBM sees the plan's
 // segments once (2 B per event instead of the reference's 4 B int32 index) and the output
@@ -32,6 +33,7 @@ namespace bp {
 constexpr int kCompactRows = 4096;  // rows per compaction block (256 threads x 16)
 constexpr int kTiledThreads = 1024;
 constexpr int kBlockGroup = 1024;   // compaction blocks scanned per group
+constexpr size_t kStaticSmemReserve = 1024;  // the kernel's static shared variables
 
 // ---------------------------------------------------------------------------
 // plan build: one CTA per row (grid-stride)
@@ -39,19 +41,18 @@ constexpr int kBlockGroup = 1024;   // compaction blocks scanned per group
 template <typename IdxT>
 __global__ void __launch_bounds__(256) plan_build_kernel(const IdxT* __restrict__ indptr, const IdxT* __restrict__ indices,
                                                          const float* __restrict__ data, int64_t nnz, int64_t m,
-                                                         int64_t n, int tile_w, int nt, uint64_t* __restrict__ row_start,
-                                                         uint32_t* __restrict__ tile_off, uint16_t* __restrict__ idx,
-                                                         float* __restrict__ w) {
+                                                         int64_t n, int tile_w, int nt, uint32_t* __restrict__ seg_off,
+                                                         uint16_t* __restrict__ idx, float* __restrict__ w) {
   extern __shared__ uint32_t sm[];
-  uint32_t* hist = sm;            // nt
-  uint32_t* offs = sm + nt;       // nt + 1
+  uint32_t* hist = sm;               // nt
+  uint32_t* offs = sm + nt;          // nt + 1
   uint32_t* cursor = offs + nt + 1;  // nt
-  const uint64_t per_row = 4ull * (uint64_t)nt + 4ull;
+  const uint64_t per_row = 8ull * (uint64_t)nt + 8ull;
   for (int64_t row = blockIdx.x; row < m; row += gridDim.x) {
     int64_t b = (int64_t)indptr[row], e = (int64_t)indptr[row + 1];
     b = b < 0 ? 0 : (b > nnz ? nnz : b);
     e = e < b ? b : (e > nnz ? nnz : e);
-    const uint64_t rs = (((uint64_t)b + 3ull) & ~3ull) + per_row * (uint64_t)row;
+    const uint64_t rs = (((uint64_t)b + 7ull) & ~7ull) + per_row * (uint64_t)row;  // a multiple of 8
     for (int t = threadIdx.x; t < nt; t += blockDim.x) {
       hist[t] = 0;
       cursor[t] = 0;
@@ -66,13 +67,13 @@ __global__ void __launch_bounds__(256) plan_build_kernel(const IdxT* __restrict_
       uint32_t acc = 0;
       for (int t = 0; t < nt; ++t) {
         offs[t] = acc;
-        acc += (hist[t] + 3u) & ~3u;
+        acc += (hist[t] + 7u) & ~7u;
       }
       offs[nt] = acc;
-      row_start[row] = rs;
     }
     __syncthreads();
-    for (int t = threadIdx.x; t <= nt; t += blockDim.x) tile_off[row * (int64_t)(nt + 1) + t] = offs[t];
+    for (int t = threadIdx.x; t <= nt; t += blockDim.x)
+      seg_off[row * (int64_t)(nt + 1) + t] = (uint32_t)((rs + offs[t]) >> 3);
     for (int64_t j = b + threadIdx.x; j < e; j += blockDim.x) {
       int64_t c = (int64_t)indices[j];
       if (c < 0 || c >= n) continue;
@@ -83,7 +84,7 @@ __global__ void __launch_bounds__(256) plan_build_kernel(const IdxT* __restrict_
       if (w) w[dst] = data[j];
     }
     for (int t = threadIdx.x; t < nt; t += blockDim.x) {
-      uint32_t h = hist[t], hp = (h + 3u) & ~3u;
+      uint32_t h = hist[t], hp = (h + 7u) & ~7u;
       for (uint32_t p = h; p < hp; ++p) {
         uint64_t dst = rs + offs[t] + p;
         idx[dst] = kPadIndex;
@@ -138,24 +139,20 @@ __global__ void __launch_bounds__(256) compact_blocked_kernel(const void* __rest
 // ---------------------------------------------------------------------------
 // tiled accumulation
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ uint2 ld_stream_u2(const uint16_t* p) {
-  return __ldcs(reinterpret_cast<const uint2*>(p));
-}
-__device__ __forceinline__ float4 ld_stream_f4(const float* p) { return __ldcs(reinterpret_cast<const float4*>(p)); }
-
-// Accumulation modes of the tiled kernel:
-//   kCount  homogeneous weight, events: uint32 event counts, out = (float)count * w
+// Accumulation modes:
+//   kCount  homogeneous weight, events: uint32 count per column, out = (float)count * w
 //   kWeight heterogeneous weights, events: float32 sum of w_ij
 //   kRowVal homogeneous weight, dense vector x: float32 sum of x_i, out = w * sum
 //   kWRow   heterogeneous weights, dense vector x: float32 sum of w_ij * x_i
 enum { kCount = 0, kWeight = 1, kRowVal = 2, kWRow = 3 };
 
 template <int MODE>
-__device__ __forceinline__ void accumulate4(uint32_t* acc, uint2 v, float4 wv, float xv, uint32_t tile_w) {
-  uint32_t x[4] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16};
-  float ww[4] = {wv.x, wv.y, wv.z, wv.w};
+__device__ __forceinline__ void accumulate8(uint32_t* acc, uint4 v, float4 w0, float4 w1, float xv, uint32_t tile_w) {
+  const uint32_t x[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
+                         v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
+  const float ww[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 0; q < 8; ++q) {
     if (x[q] < tile_w) {  // excludes the 0xFFFF padding
       if (MODE == kCount) atomicAdd(acc + x[q], 1u);
       else if (MODE == kWeight) atomicAdd(reinterpret_cast<float*>(acc) + x[q], ww[q]);
@@ -165,9 +162,14 @@ __device__ __forceinline__ void accumulate4(uint32_t* acc, uint2 v, float4 wv, f
   }
 }
 
+__device__ __forceinline__ uint4 ld_stream_u4(const uint16_t* p) { return __ldcs(reinterpret_cast<const uint4*>(p)); }
+__device__ __forceinline__ float4 ld_stream_f4(const float* p) { return __ldcs(reinterpret_cast<const float4*>(p)); }
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 struct TiledArgs {
-  const uint64_t* row_start;
-  const uint32_t* tile_off;
+  const uint32_t* seg_off;
   const uint16_t* idx;
   const float* w;
   const int32_t* lists;
@@ -181,34 +183,37 @@ struct TiledArgs {
 };
 
 // Warp-independent processing: after one CTA-wide prefix over this rank's compaction blocks,
-// every warp walks "slices" of 32 active rows.  Lane l of a slice owns row 32k+l and fetches
-// its segment descriptor (start, chunk count) for this CTA's tile; the row ids of slice k+2W
-// and the descriptors of slice k+W are in flight while slice k is processed.  Inside a slice,
-// groups of G lanes take one segment each (lane gl loads 8-byte chunk gl, 4 uint16 indices)
-// and G segments are loaded back to back before any shared-memory atomic is issued.
-template <int MODE, int G, int RND>
-__global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArgs a) {
+// every warp walks "slices" of 32 active rows (slices warp, warp + W, ...).  Lane l of a slice
+// owns row 32k + l and loads that row's segment bounds for this CTA's tile.  Pipeline per
+// warp: the row ids of slice k + 3W and the segment bounds of slice k + 2W are loaded, the
+// segments of slice k + W are prefetched into L2 (PF), and slice k is processed: groups of G
+// lanes take one segment each (lane gl loads 16-byte chunks gl, gl + G, ... -- RND rounds, 8
+// tile-local indices per chunk) and UB segments per group are loaded back to back before any
+// shared-memory atomic is issued.
+template <int MODE, int G, int RND, bool PF>
+__global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const TiledArgs a) {
   constexpr bool HAS_W = (MODE == kWeight || MODE == kWRow);
   constexpr bool HAS_X = (MODE == kRowVal || MODE == kWRow);
-  extern __shared__ uint4 smem_raw[];
-  uint32_t* acc = reinterpret_cast<uint32_t*>(smem_raw);
-  int* s_boff = reinterpret_cast<int*>(acc + a.acc_words);  // kBlockGroup + 1
+  constexpr unsigned FULL = 0xffffffffu;
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint32_t* acc = reinterpret_cast<uint32_t*>(smem);
+  int* s_boff = reinterpret_cast<int*>(smem + sizeof(uint32_t) * (size_t)a.acc_words);  // kBlockGroup + 1
   __shared__ int s_wsum[32];
 
   cg::cluster_group cluster = cg::this_cluster();
   const int R = (int)cluster.num_blocks();
   const int rank = (int)cluster.block_rank();
   const int tile = blockIdx.x / R;
-  const int tid = threadIdx.x;
-  const int nthr = blockDim.x;
+  const int tid = threadIdx.x, nthr = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
 
-  for (int i = tid; i < a.acc_words; i += nthr) acc[i] = 0u;
+  {
+    uint4* acc4 = reinterpret_cast<uint4*>(acc);
+    for (int i = tid; i < (a.acc_words >> 2); i += nthr) acc4[i] = make_uint4(0u, 0u, 0u, 0u);
+  }
 
   const int b0 = (int)((int64_t)rank * a.nb / R), b1 = (int)((int64_t)(rank + 1) * a.nb / R);
-  const uint64_t* __restrict__ row_start = a.row_start;
-  const uint32_t* __restrict__ tile_off = a.tile_off;
-  const int64_t toff_stride = a.n_tiles + 1;
+  const int64_t so_stride = a.n_tiles + 1;
 
   // the compaction kernel of this call may still be running (programmatic dependent launch)
   cudaGridDependencySynchronize();
@@ -220,7 +225,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArg
     int incl = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      int t = __shfl_up_sync(0xffffffffu, incl, o);
+      int t = __shfl_up_sync(FULL, incl, o);
       if (lane >= o) incl += t;
     }
     if (lane == 31) s_wsum[warp] = incl;
@@ -229,7 +234,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArg
       int t = s_wsum[lane], ti = t;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        int u = __shfl_up_sync(0xffffffffu, ti, o);
+        int u = __shfl_up_sync(FULL, ti, o);
         if (lane >= o) ti += u;
       }
       s_wsum[lane] = ti - t;
@@ -241,16 +246,6 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArg
     const int total = s_boff[ng];
     const int nslices = (total + 31) >> 5;
 
-    // Lane-per-segment: in slice k (elements 32k .. 32k+31 of this rank's active-row list),
-    // lane l owns row 32k+l and walks that row's segment for this tile on its own, so the
-    // inner loop issues only global loads and shared-memory atomics (no shuffles).
-    // row id of element g of this group's list; `blk` is the lane's running block hint
-    auto fetch_row = [&](int k, int& blk) -> int32_t {
-      const int g = (k << 5) + lane;
-      if (k >= nslices || g >= total) return -1;
-      while (s_boff[blk + 1] <= g) ++blk;  // blocks hold ~rate*4096 rows: a step or two
-      return __ldg(a.lists + (int64_t)(g0 + blk) * kCompactRows + (g - s_boff[blk]));
-    };
     auto block_of = [&](int g) -> int {
       int lo = 0, hi = ng;
       while (hi - lo > 1) {
@@ -260,65 +255,74 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArg
       }
       return lo;
     };
+    // row id of element 32k + lane of the group's list (-1 past the end); `blk` is the lane's
+    // running block hint (the lane's elements only grow)
+    auto fetch_row = [&](int k, int& blk) -> int32_t {
+      const int g = (k << 5) + lane;
+      if (k >= nslices || g >= total) return -1;
+      while (s_boff[blk + 1] <= g) ++blk;  // blocks hold ~rate*4096 rows: a step or two
+      return __ldg(a.lists + (int64_t)(g0 + blk) * kCompactRows + (g - s_boff[blk]));
+    };
     auto fetch_desc = [&](int32_t row, uint32_t& st, uint32_t& nch, float& xv) {
       st = 0;
       nch = 0;
       xv = 0.0f;
       if (row >= 0) {
+        const uint32_t* so = a.seg_off + (int64_t)row * so_stride + tile;
+        st = __ldg(so);
+        nch = __ldg(so + 1) - st;
         if (HAS_X) xv = __ldg(a.row_val + row);
-        const uint64_t rs = __ldg(row_start + row);
-        const uint32_t* to = tile_off + (int64_t)row * toff_stride + tile;
-        const uint32_t o0 = __ldg(to), o1 = __ldg(to + 1);
-        st = (uint32_t)(rs + o0);
-        nch = (o1 - o0) >> 2;
       }
     };
 
+    const int gmax = max(total - 1, 0);
     int k = warp;
-    int blk1 = block_of(min((k << 5) + lane, max(total - 1, 0)));
-    uint32_t cst, cn;
-    float cxv;
-    fetch_desc(fetch_row(k, blk1), cst, cn, cxv);
-    int blk2 = block_of(min(((k + nwarps) << 5) + lane, max(total - 1, 0)));
-    int32_t row1 = fetch_row(k + nwarps, blk2);
-    int blk3 = blk2;
+    int blk = block_of(min((k << 5) + lane, gmax));
+    uint32_t cst, cn, nst, nn, mst, mn;
+    float cxv, nxv, mxv;
+    fetch_desc(fetch_row(k, blk), cst, cn, cxv);                 // slice k
+    fetch_desc(fetch_row(k + nwarps, blk), nst, nn, nxv);        // slice k + W
+    int32_t row2 = fetch_row(k + 2 * nwarps, blk);               // slice k + 2W
     while (k < nslices) {
-      uint32_t nst, nn;
-      float nxv;
-      fetch_desc(row1, nst, nn, nxv);  // slice k + W: in flight during slice k
-      int32_t row2 = -1;
-      if (k + 2 * nwarps < nslices) {
-        blk3 = block_of(min(((k + 2 * nwarps) << 5) + lane, max(total - 1, 0)));
-        row2 = fetch_row(k + 2 * nwarps, blk3);
+      fetch_desc(row2, mst, mn, mxv);                            // slice k + 2W
+      row2 = fetch_row(k + 3 * nwarps, blk);                     // slice k + 3W
+      if (PF) {
+        // slice k + W into L2: one prefetch per 32-byte sector of the lane's segment
+        for (uint32_t c = 0; c < nn; c += 2) {
+          prefetch_l2(a.idx + 8ull * (nst + c));
+          if (HAS_W) {
+            prefetch_l2(a.w + 8ull * (nst + c));
+            prefetch_l2(a.w + 8ull * (nst + c) + 8);
+          }
+        }
       }
-      // Groups of G lanes share a segment: group grp takes the segments of lanes
-      // grp, grp + 32/G, ...; lane gl of the group loads chunks gl, gl + G, ... (RND rounds),
-      // so one warp-wide load touches 32/G segments with G consecutive chunks each.  UB
-      // segments are loaded before any of their atomics are issued.
       {
         constexpr int NG = 32 / G;
-        constexpr int UBMAX = (HAS_W ? 4 : 8) / RND > 0 ? (HAS_W ? 4 : 8) / RND : 1;
+        constexpr int UBMAX = (HAS_W ? 2 : 4) / RND > 0 ? (HAS_W ? 2 : 4) / RND : 1;
         constexpr int UB = UBMAX > G ? G : UBMAX;
         const int grp = lane / G, gl = lane % G;
 #pragma unroll 1
         for (int u0 = 0; u0 < G; u0 += UB) {
-          uint2 vv[UB][RND];
-          float4 wv[UB][RND];
+          uint4 vv[UB][RND];
+          float4 w0[UB][RND], w1[UB][RND];
           uint32_t st[UB], ln[UB];
           float xs[UB];
 #pragma unroll
           for (int u = 0; u < UB; ++u) {
             const int j = grp + (u0 + u) * NG;
-            st[u] = __shfl_sync(0xffffffffu, cst, j);
-            ln[u] = __shfl_sync(0xffffffffu, cn, j);
-            xs[u] = HAS_X ? __shfl_sync(0xffffffffu, cxv, j) : 0.0f;
+            st[u] = __shfl_sync(FULL, cst, j);
+            ln[u] = __shfl_sync(FULL, cn, j);
+            xs[u] = HAS_X ? __shfl_sync(FULL, cxv, j) : 0.0f;
 #pragma unroll
             for (int r = 0; r < RND; ++r) {
               const uint32_t c = gl + r * G;
               if (c < ln[u]) {
-                const uint32_t e = st[u] + 4u * c;
-                vv[u][r] = ld_stream_u2(a.idx + e);
-                if (HAS_W) wv[u][r] = ld_stream_f4(a.w + e);
+                const uint64_t e = 8ull * (st[u] + c);
+                vv[u][r] = ld_stream_u4(a.idx + e);
+                if (HAS_W) {
+                  w0[u][r] = ld_stream_f4(a.w + e);
+                  w1[u][r] = ld_stream_f4(a.w + e + 4);
+                }
               }
             }
           }
@@ -327,15 +331,20 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArg
 #pragma unroll
             for (int r = 0; r < RND; ++r)
               if (gl + r * G < ln[u])
-                accumulate4<MODE>(acc, vv[u][r], HAS_W ? wv[u][r] : make_float4(0, 0, 0, 0), xs[u], a.tile_w);
-          // chunks beyond RND*G (long segments): rare, plain loop
+                accumulate8<MODE>(acc, vv[u][r], HAS_W ? w0[u][r] : make_float4(0, 0, 0, 0),
+                                  HAS_W ? w1[u][r] : make_float4(0, 0, 0, 0), xs[u], (uint32_t)a.tile_w);
+          // chunks beyond RND*G (long segments)
 #pragma unroll
           for (int u = 0; u < UB; ++u) {
             for (uint32_t c = gl + RND * G; c < ln[u]; c += G) {
-              const uint32_t e = st[u] + 4u * c;
-              const uint2 x = ld_stream_u2(a.idx + e);
-              const float4 y = HAS_W ? ld_stream_f4(a.w + e) : make_float4(0, 0, 0, 0);
-              accumulate4<MODE>(acc, x, y, xs[u], a.tile_w);
+              const uint64_t e = 8ull * (st[u] + c);
+              const uint4 x = ld_stream_u4(a.idx + e);
+              float4 y0 = make_float4(0, 0, 0, 0), y1 = y0;
+              if (HAS_W) {
+                y0 = ld_stream_f4(a.w + e);
+                y1 = ld_stream_f4(a.w + e + 4);
+              }
+              accumulate8<MODE>(acc, x, y0, y1, xs[u], (uint32_t)a.tile_w);
             }
           }
         }
@@ -343,7 +352,9 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArg
       cst = nst;
       cn = nn;
       cxv = nxv;
-      row1 = row2;
+      nst = mst;
+      nn = mn;
+      nxv = mxv;
       k += nwarps;
     }
   }
@@ -355,15 +366,21 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArg
   const float w = (MODE == kCount || MODE == kRowVal) ? __ldg(a.w_homo) : 0.0f;
   const int64_t col_base = (int64_t)tile * a.tile_w;
   for (int c = c0 + 4 * tid; c < c0 + slice; c += 4 * nthr) {
+    uint4 x[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r)
+      if (r < R) x[r] = *reinterpret_cast<const uint4*>(cluster.map_shared_rank(acc, r) + c);
     float o[4];
     if (MODE == kCount) {
       uint4 s = make_uint4(0, 0, 0, 0);
-      for (int r = 0; r < R; ++r) {
-        const uint4 x = *reinterpret_cast<const uint4*>(cluster.map_shared_rank(acc, r) + c);
-        s.x += x.x;
-        s.y += x.y;
-        s.z += x.z;
-        s.w += x.w;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        if (r < R) {
+          s.x += x[r].x;
+          s.y += x[r].y;
+          s.z += x[r].z;
+          s.w += x[r].w;
+        }
       }
       o[0] = (float)s.x * w;
       o[1] = (float)s.y * w;
@@ -371,12 +388,14 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArg
       o[3] = (float)s.w * w;
     } else {
       float4 s = make_float4(0, 0, 0, 0);
-      for (int r = 0; r < R; ++r) {
-        const float4 x = *reinterpret_cast<const float4*>(cluster.map_shared_rank(acc, r) + c);
-        s.x += x.x;
-        s.y += x.y;
-        s.z += x.z;
-        s.w += x.w;
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        if (r < R) {
+          s.x += __uint_as_float(x[r].x);
+          s.y += __uint_as_float(x[r].y);
+          s.z += __uint_as_float(x[r].z);
+          s.w += __uint_as_float(x[r].w);
+        }
       }
       if (MODE == kRowVal) {
         s.x = __fmul_rn(w, s.x);
@@ -400,6 +419,19 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(TiledArg
   cluster.sync();
 }
 
+static int max_smem_optin() {
+  static int cache[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (cache[dev] == 0) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cache[dev] = v > 0 ? v : 227 * 1024;
+  }
+  return cache[dev];
+}
+
 static size_t tiled_smem_bytes(int acc_words) {
   return sizeof(uint32_t) * (size_t)acc_words + sizeof(int) * (kBlockGroup + 1);
 }
@@ -409,23 +441,30 @@ static int acc_words_for(int tile_w, int R) {
   return (tile_w + q - 1) / q * q;
 }
 
-template <int MODE, int G, int RND>
-static bp_status launch_tiled_g(const TiledArgs& a, int R, cudaStream_t st) {
-  auto kfn = ecsr_t_tiled_kernel<MODE, G, RND>;
-  const size_t smem = tiled_smem_bytes(a.acc_words);
-  static thread_local size_t configured[64] = {0};
+// Raises a kernel's dynamic shared-memory limit to the largest size any launch uses (once per
+// device and instantiation; every caller sets the same value, so none can lower it).
+template <typename K>
+static cudaError_t prepare_kernel(K kfn, bool* done) {
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) dev = 0;
-  if (configured[dev] < smem) {
-    BP_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    BP_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-    configured[dev] = smem;
-  }
+  if (done[dev]) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       max_smem_optin() - (int)kStaticSmemReserve);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(kfn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e == cudaSuccess) done[dev] = true;
+  return e;
+}
+
+template <int MODE, int G, int RND, bool PF>
+static bp_status launch_tiled_g(const TiledArgs& a, int R, cudaStream_t st) {
+  auto kfn = ecsr_t_tiled_kernel<MODE, G, RND, PF>;
+  static bool done[64] = {false};
+  BP_CUDA_TRY(prepare_kernel(kfn, done));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(a.n_tiles * R), 1, 1);
   cfg.blockDim = dim3(kTiledThreads, 1, 1);
-  cfg.dynamicSmemBytes = smem;
+  cfg.dynamicSmemBytes = tiled_smem_bytes(a.acc_words);
   cfg.stream = st;
   cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -440,37 +479,44 @@ static bp_status launch_tiled_g(const TiledArgs& a, int R, cudaStream_t st) {
   return BP_OK;
 }
 
-// (lanes per segment, chunk rounds) from the mean segment length in 8-byte chunks; the
-// environment variable BPGPU_TILED_GROUP=G,RND overrides (tuning).
-static void choose_group(double chunks, int& G, int& RND) {
-  if (chunks <= 1.5) { G = 1; RND = 2; }
-  else if (chunks <= 4.5) { G = 2; RND = 2; }
-  else if (chunks <= 10.0) { G = 4; RND = 2; }
-  else if (chunks <= 14.0) { G = 4; RND = 3; }
+// (lanes per segment, chunk rounds, L2 prefetch) from the mean segment length in 16-byte
+// chunks; BPGPU_TILED=G,RND,PF overrides (tuning).
+static void tiled_config(double chunks, int& G, int& RND, int& PF) {
+  if (chunks <= 1.25) { G = 1; RND = 1; }
+  else if (chunks <= 2.5) { G = 2; RND = 1; }
+  else if (chunks <= 5.0) { G = 4; RND = 1; }
+  else if (chunks <= 9.0) { G = 8; RND = 1; }
   else { G = 8; RND = 2; }
-  static int env_g = -1, env_r = -1;
-  if (env_g < 0) {
-    env_g = 0;
-    const char* e = getenv("BPGPU_TILED_GROUP");
-    if (e) sscanf(e, "%d,%d", &env_g, &env_r);
+  PF = 0;  // measured: L2 prefetch of the next slice does not pay at 2-10 % event rates
+  static int env[3] = {-1, -1, -1};
+  if (env[0] < 0) {
+    env[0] = 0;
+    const char* e = getenv("BPGPU_TILED");
+    if (e) sscanf(e, "%d,%d,%d", &env[0], &env[1], &env[2]);
   }
-  if (env_g > 0) {
-    G = env_g;
-    RND = env_r > 0 ? env_r : 2;
+  if (env[0] > 0) {
+    G = env[0];
+    RND = env[1] > 0 ? env[1] : 1;
+    PF = env[2] != 0;
   }
 }
 
 template <int MODE>
 static bp_status launch_tiled(const TiledArgs& a, int R, double chunks, cudaStream_t st) {
-  int G, RND;
-  choose_group(chunks, G, RND);
-  if (G == 1) return launch_tiled_g<MODE, 1, 2>(a, R, st);
-  if (G == 2) return launch_tiled_g<MODE, 2, 2>(a, R, st);
-  if (G == 4 && RND == 2) return launch_tiled_g<MODE, 4, 2>(a, R, st);
-  if (G == 4) return launch_tiled_g<MODE, 4, 3>(a, R, st);
-  if (G == 8 && RND == 1) return launch_tiled_g<MODE, 8, 1>(a, R, st);
-  if (G == 8) return launch_tiled_g<MODE, 8, 2>(a, R, st);
-  return launch_tiled_g<MODE, 16, 1>(a, R, st);
+  int G, RND, PF;
+  tiled_config(chunks, G, RND, PF);
+#define BP_TILED_CASE(g, r)                                                                   \
+  if (G == g && RND == r)                                                                     \
+    return PF ? launch_tiled_g<MODE, g, r, true>(a, R, st) : launch_tiled_g<MODE, g, r, false>(a, R, st);
+  BP_TILED_CASE(1, 1)
+  BP_TILED_CASE(2, 1)
+  BP_TILED_CASE(4, 1)
+  BP_TILED_CASE(2, 2)
+  BP_TILED_CASE(8, 1)
+  BP_TILED_CASE(8, 2)
+#undef BP_TILED_CASE
+  set_error("tiled event kernel: no variant G=%d RND=%d", G, RND);
+  return BP_ENOTSUP;
 }
 
 template <int ET>
@@ -491,10 +537,14 @@ static bp_status compact_blocked(const void* events, bp_etype et, int64_t m, int
   return BP_EINVAL;
 }
 
+// how many clusters of R CTAs with `smem` bytes of shared memory can be resident at once
 static int max_active_clusters(int R, size_t smem) {
-  auto kfn = ecsr_t_tiled_kernel<kCount, 4, 3>;
-  if (cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
-  cudaFuncSetAttribute(kfn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  auto kfn = ecsr_t_tiled_kernel<kCount, 4, 1, true>;
+  static bool done[64] = {false};
+  if (prepare_kernel(kfn, done) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(R * 64), 1, 1);
   cfg.blockDim = dim3(kTiledThreads, 1, 1);
@@ -514,17 +564,25 @@ static int max_active_clusters(int R, size_t smem) {
   return num;
 }
 
-static int max_smem_optin() {
-  static int cache[64] = {0};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 0 || dev >= 64) dev = 0;
-  if (cache[dev] == 0) {
-    int v = 0;
-    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cache[dev] = v > 0 ? v : 227 * 1024;
-  }
-  return cache[dev];
+// fills the plan-dependent kernel arguments; checks the tile fits shared memory
+static bp_status tiled_args_from_plan(const bp_csr_plan* plan, int cluster, TiledArgs& a, double& chunks,
+                                      const char* who) {
+  const int acc_words = acc_words_for(plan->tile_w, cluster);
+  BP_REQUIRE(tiled_smem_bytes(acc_words) <= (size_t)max_smem_optin() - kStaticSmemReserve, BP_ENOTSUP,
+             "%s: tile of %d columns does not fit shared memory", who, plan->tile_w);
+  PlanView v = plan_view(plan);
+  a = TiledArgs{};
+  a.seg_off = v.seg_off;
+  a.idx = v.idx;
+  a.w = v.w;
+  a.n = plan->n;
+  a.tile_w = plan->tile_w;
+  a.n_tiles = plan->n_tiles;
+  a.nb = (int)((plan->m + kCompactRows - 1) / kCompactRows);
+  a.acc_words = acc_words;
+  // mean segment length in chunks: entries per (row, tile) plus the average padding
+  chunks = ((double)plan->nnz / (double)std::max<int64_t>(plan->m, 1) / (double)plan->n_tiles + 3.5) / 8.0;
+  return BP_OK;
 }
 
 }  // namespace bp
@@ -536,10 +594,11 @@ extern "C" {
 int32_t bp_csr_plan_default_tile(int64_t n, int32_t cluster) {
   if (n <= 0) return 0;
   if (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8) cluster = 4;
-  const int64_t cap_words = (int64_t)(max_smem_optin() - 4 * (kBlockGroup + 1) - 1024) / 4;
+  const int64_t cap_words =
+      ((int64_t)max_smem_optin() - (int64_t)kStaticSmemReserve - 4 * (kBlockGroup + 1)) / 4;
   const int64_t cap_tw = std::min<int64_t>(cap_words / 64 * 64, kPlanMaxTileW / 64 * 64);
   // how many clusters of `cluster` CTAs (one CTA per SM) can be resident at once
-  int clusters = max_active_clusters(cluster, tiled_smem_bytes((int)cap_tw));
+  int clusters = max_active_clusters(cluster, tiled_smem_bytes(acc_words_for((int)cap_tw, cluster)));
   if (clusters < 1) clusters = std::max(1, device_sm_count() / cluster);
   int64_t tw = (n + clusters - 1) / clusters;
   tw = (tw + 63) / 64 * 64;
@@ -572,9 +631,10 @@ bp_status bp_csr_plan_build(const float* data, int64_t ndata, const void* indice
   BP_REQUIRE(!heter || ndata == nnz, BP_ESHAPE, "csr_plan_build: data size %lld != nnz %lld", (long long)ndata,
              (long long)nnz);
   PlanLayout L = plan_layout(m, nnz, (int32_t)nt, heter);
-  BP_REQUIRE(L.entries < (1ull << 32), BP_ENOTSUP, "csr_plan_build: %llu padded entries exceed 2^32",
-             (unsigned long long)L.entries);
+  BP_REQUIRE(L.chunks < (1ull << 32), BP_ENOTSUP, "csr_plan_build: %llu padded 16-byte chunks exceed 2^32",
+             (unsigned long long)L.chunks);
   BP_REQUIRE(mem != nullptr && bytes >= L.total, BP_ENOMEM, "csr_plan_build: memory %zu < %zu", bytes, L.total);
+  BP_REQUIRE((reinterpret_cast<uintptr_t>(mem) & 255u) == 0, BP_EINVAL, "csr_plan_build: memory not 256-byte aligned");
   BP_REQUIRE(m == 0 || (indices && indptr) || nnz == 0, BP_EINVAL, "csr_plan_build: null indices/indptr");
   bp_csr_plan p = {};
   p.m = m;
@@ -587,25 +647,23 @@ bp_status bp_csr_plan_build(const float* data, int64_t ndata, const void* indice
   p.mem = mem;
   p.bytes = bytes;
   char* base = static_cast<char*>(mem);
-  uint64_t* rs = reinterpret_cast<uint64_t*>(base + L.off_row_start);
-  uint32_t* toff = reinterpret_cast<uint32_t*>(base + L.off_tile_off);
+  uint32_t* so = reinterpret_cast<uint32_t*>(base + L.off_seg);
   uint16_t* idx = reinterpret_cast<uint16_t*>(base + L.off_idx);
   float* w = heter ? reinterpret_cast<float*>(base + L.off_w) : nullptr;
   if (m > 0) {
     if (nnz == 0) {
-      BP_CUDA_TRY(cudaMemsetAsync(toff, 0, sizeof(uint32_t) * (size_t)m * (size_t)(nt + 1), st));
-      BP_CUDA_TRY(cudaMemsetAsync(rs, 0, sizeof(uint64_t) * (size_t)m, st));
+      BP_CUDA_TRY(cudaMemsetAsync(so, 0, sizeof(uint32_t) * (size_t)m * (size_t)(nt + 1), st));
     } else {
       int grid = (int)std::min<int64_t>(m, (int64_t)device_sm_count() * 16);
       size_t smem = sizeof(uint32_t) * (size_t)(3 * nt + 1);
       if (itype == BP_I32)
         plan_build_kernel<int32_t><<<grid, 256, smem, st>>>(static_cast<const int32_t*>(indptr),
                                                              static_cast<const int32_t*>(indices), data, nnz, m, n,
-                                                             tile_w, (int)nt, rs, toff, idx, w);
+                                                             tile_w, (int)nt, so, idx, w);
       else
         plan_build_kernel<int64_t><<<grid, 256, smem, st>>>(static_cast<const int64_t*>(indptr),
                                                              static_cast<const int64_t*>(indices), data, nnz, m, n,
-                                                             tile_w, (int)nt, rs, toff, idx, w);
+                                                             tile_w, (int)nt, so, idx, w);
       bp_status s = check_launch("plan_build_kernel");
       if (s != BP_OK) return s;
     }
@@ -614,13 +672,12 @@ bp_status bp_csr_plan_build(const float* data, int64_t ndata, const void* indice
   return BP_OK;
 }
 
-bp_status bp_csr_plan_arrays(const bp_csr_plan* plan, const uint64_t** row_start, const uint32_t** tile_off,
-                             const uint16_t** idx, const float** w) {
+bp_status bp_csr_plan_arrays(const bp_csr_plan* plan, const uint32_t** seg_off, const uint16_t** idx,
+                             const float** w) {
   clear_error();
   BP_REQUIRE(plan != nullptr && plan->mem != nullptr, BP_EINVAL, "csr_plan_arrays: null plan");
   PlanView v = plan_view(plan);
-  if (row_start) *row_start = v.row_start;
-  if (tile_off) *tile_off = v.tile_off;
+  if (seg_off) *seg_off = v.seg_off;
   if (idx) *idx = v.idx;
   if (w) *w = v.w;
   return BP_OK;
@@ -656,41 +713,24 @@ bp_status bp_event_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, c
   BP_REQUIRE(workspace && workspace_bytes >= bp_event_csrmv_planned_workspace_size(plan), BP_ENOMEM,
              "event_csrmv_planned: workspace %zu < %zu", workspace_bytes,
              bp_event_csrmv_planned_workspace_size(plan));
-  const int acc_words = acc_words_for(plan->tile_w, cluster);
-  BP_REQUIRE(tiled_smem_bytes(acc_words) <= (size_t)max_smem_optin(), BP_ENOTSUP,
-             "event_csrmv_planned: tile of %d columns does not fit shared memory", plan->tile_w);
-  const int nb = (int)((m + kCompactRows - 1) / kCompactRows);
+  TiledArgs a;
+  double chunks = 0.0;
+  bp_status s = tiled_args_from_plan(plan, cluster, a, chunks, "event_csrmv_planned");
+  if (s != BP_OK) return s;
   int32_t* lists = static_cast<int32_t*>(workspace);
   int32_t* counts = reinterpret_cast<int32_t*>(static_cast<char*>(workspace) +
-                                               align_up(sizeof(int32_t) * (size_t)nb * kCompactRows, 256));
+                                               align_up(sizeof(int32_t) * (size_t)a.nb * kCompactRows, 256));
   ScopedKernelTimer tk(st);  // brackets both kernels of the call
-  bp_status s = compact_blocked(events, etype, m, lists, counts, st);
+  s = compact_blocked(events, etype, m, lists, counts, st);
   if (s != BP_OK) return s;
-  PlanView v = plan_view(plan);
-  TiledArgs a;
-  a.row_start = v.row_start;
-  a.tile_off = v.tile_off;
-  a.idx = v.idx;
-  a.w = v.w;
   a.lists = lists;
   a.counts = counts;
   a.w_homo = w_homo;
   a.row_val = nullptr;
   a.out = out;
-  a.n = n;
-  a.tile_w = plan->tile_w;
-  a.n_tiles = plan->n_tiles;
-  a.nb = nb;
-  a.acc_words = acc_words;
   a.vec_out = ((reinterpret_cast<uintptr_t>(out) & 15u) == 0) ? 1 : 0;
-  const double chunks = ((double)plan->nnz / (double)m / (double)plan->n_tiles + 1.5) / 4.0;
-  s = homo ? launch_tiled<kCount>(a, cluster, chunks, st) : launch_tiled<kWeight>(a, cluster, chunks, st);
-  return s;
+  return homo ? launch_tiled<kCount>(a, cluster, chunks, st) : launch_tiled<kWeight>(a, cluster, chunks, st);
 }
-
-}  // extern "C"
-
-extern "C" {
 
 // sparse.csrmv, transpose=1, on a plan: out[j] = sum_i A[i, j] * vec[i].  Rows with vec[i] == 0
 // contribute nothing and are skipped by the compaction (the dense vector is treated as
@@ -715,34 +755,22 @@ bp_status bp_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, const f
   BP_REQUIRE(!homo || w_homo != nullptr, BP_EINVAL, "csrmv_planned: homogeneous plan needs w_homo");
   BP_REQUIRE(workspace && workspace_bytes >= bp_event_csrmv_planned_workspace_size(plan), BP_ENOMEM,
              "csrmv_planned: workspace %zu < %zu", workspace_bytes, bp_event_csrmv_planned_workspace_size(plan));
-  const int acc_words = acc_words_for(plan->tile_w, cluster);
-  BP_REQUIRE(tiled_smem_bytes(acc_words) <= (size_t)max_smem_optin(), BP_ENOTSUP,
-             "csrmv_planned: tile of %d columns does not fit shared memory", plan->tile_w);
-  const int nb = (int)((m + kCompactRows - 1) / kCompactRows);
+  TiledArgs a;
+  double chunks = 0.0;
+  bp_status s = tiled_args_from_plan(plan, cluster, a, chunks, "csrmv_planned");
+  if (s != BP_OK) return s;
   int32_t* lists = static_cast<int32_t*>(workspace);
   int32_t* counts = reinterpret_cast<int32_t*>(static_cast<char*>(workspace) +
-                                               align_up(sizeof(int32_t) * (size_t)nb * kCompactRows, 256));
+                                               align_up(sizeof(int32_t) * (size_t)a.nb * kCompactRows, 256));
   ScopedKernelTimer tk(st);
-  bp_status s = compact_blocked(vec, BP_EV_F32_NZ, m, lists, counts, st);
+  s = compact_blocked(vec, BP_EV_F32_NZ, m, lists, counts, st);
   if (s != BP_OK) return s;
-  PlanView v = plan_view(plan);
-  TiledArgs a;
-  a.row_start = v.row_start;
-  a.tile_off = v.tile_off;
-  a.idx = v.idx;
-  a.w = v.w;
   a.lists = lists;
   a.counts = counts;
   a.w_homo = w_homo;
   a.row_val = vec;
   a.out = out;
-  a.n = n;
-  a.tile_w = plan->tile_w;
-  a.n_tiles = plan->n_tiles;
-  a.nb = nb;
-  a.acc_words = acc_words;
   a.vec_out = ((reinterpret_cast<uintptr_t>(out) & 15u) == 0) ? 1 : 0;
-  const double chunks = ((double)plan->nnz / (double)m / (double)plan->n_tiles + 1.5) / 4.0;
   return homo ? launch_tiled<kRowVal>(a, cluster, chunks, st) : launch_tiled<kWRow>(a, cluster, chunks, st);
 }
 

@@ -110,25 +110,24 @@ __global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_ne
         const int32_t kloc = *cluster.map_shared_rank(&S.list[cur][g - pre[r]], r);
         const int64_t row = (int64_t)r * tw + kloc;
         exc = row < d.n_exc;
-        const uint64_t rs = __ldg(d.row_start + row);
-        const uint32_t* to = d.tile_off + row * toff_stride + rank;
-        const uint32_t o0 = __ldg(to), o1 = __ldg(to + 1);
-        st = (uint32_t)(rs + o0);
-        nch = (o1 - o0) >> 2;
+        const uint32_t* so = d.seg_off + row * toff_stride + rank;
+        st = __ldg(so);
+        nch = __ldg(so + 1) - st;
       }
       uint32_t* acc = exc ? S.acc_e : S.acc_i;
-      constexpr int U = 8;
+      constexpr int U = 4;
       for (uint32_t c0 = 0; __any_sync(0xffffffffu, c0 < nch); c0 += U) {
-        uint2 vv[U];
+        uint4 vv[U];
 #pragma unroll
         for (int u = 0; u < U; ++u)
-          if (c0 + u < nch) vv[u] = __ldg(reinterpret_cast<const uint2*>(d.idx + st + 4u * (c0 + u)));
+          if (c0 + u < nch) vv[u] = __ldg(reinterpret_cast<const uint4*>(d.idx + 8ull * (st + c0 + u)));
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           if (c0 + u < nch) {
-            const uint32_t x[4] = {vv[u].x & 0xFFFFu, vv[u].x >> 16, vv[u].y & 0xFFFFu, vv[u].y >> 16};
+            const uint32_t x[8] = {vv[u].x & 0xFFFFu, vv[u].x >> 16, vv[u].y & 0xFFFFu, vv[u].y >> 16,
+                                   vv[u].z & 0xFFFFu, vv[u].z >> 16, vv[u].w & 0xFFFFu, vv[u].w >> 16};
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
+            for (int q = 0; q < 8; ++q)
               if (x[q] < (uint32_t)nloc) atomicAdd(acc + x[q], 1u);
           }
         }

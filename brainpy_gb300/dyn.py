@@ -131,13 +131,13 @@ class EINetwork:
 
   def descriptor(self, spike_counts=None, raster=None, v_trace=None, trace_steps=0, step_limit=0):
     plan = self._cluster_plan()
-    rs, toff, idx, w = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
-    _lib.check(_lib.lib().bp_csr_plan_arrays(ctypes.byref(plan.c), ctypes.byref(rs), ctypes.byref(toff),
-                                             ctypes.byref(idx), ctypes.byref(w)), "csr_plan_arrays")
+    so, idx, w = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    _lib.check(_lib.lib().bp_csr_plan_arrays(ctypes.byref(plan.c), ctypes.byref(so), ctypes.byref(idx),
+                                             ctypes.byref(w)), "csr_plan_arrays")
     d = _lib.NetDesc()
     d.n, d.n_exc = self.n, self.n_exc
     d.tile_w, d.n_tiles = plan.tile_w, plan.c.n_tiles
-    d.row_start, d.tile_off, d.idx = rs, toff, idx
+    d.seg_off, d.idx = so, idx
     d.we, d.wi = self.we, self.wi
     d.p = self.params.c()
     d.V, d.ge, d.gi, d.t_last = (self.V.data_ptr(), self.ge.data_ptr(), self.gi.data_ptr(), self.t_last.data_ptr())

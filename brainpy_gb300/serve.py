@@ -66,7 +66,7 @@ def job_memory(job: Job) -> int:
   k = min(int(0.02 * n), job.fanout)
   nnz = n * k
   tiles = math.ceil(n / 4096) if n <= 16 * 4096 else max(1, math.ceil(n / 27840))
-  plan = 8 * n + 4 * n * (tiles + 1) + 2 * (nnz + (4 * tiles + 4) * n + 4)
+  plan = 4 * n * (tiles + 1) + 2 * (nnz + (8 * tiles + 8) * n + 8)
   return state + 4 * nnz + 4 * (n + 1) + plan + 2 * plan
 
 

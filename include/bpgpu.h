@@ -132,7 +132,8 @@ bp_status bp_jitconn_dense(bp_jc_kind kind, float p0, float p1, int32_t clen, ui
  * Column-tiled CSR plan (no counterpart in the reference; it plays the role of a
  * cuSPARSE-style analysis step).  A one-time re-layout of a CSR matrix that the tiled
  * event kernels stream: every row's indices regrouped by column tile of tile_w columns,
- * stored as tile-local uint16 and padded to 8-byte chunks, weights permuted along.
+ * stored as tile-local uint16 and padded to 16-byte chunks (8 entries), weights permuted
+ * along.  Plans hold fewer than 2^32 chunks (about 3.4e10 entries).
  * The caller owns the device memory (bp_csr_plan_bytes) and keeps it, together with the
  * filled-in bp_csr_plan, for as long as it uses the plan.  A plan is a function of
  * (indices, indptr[, data]) at build time; rebuild it when they change.
@@ -158,9 +159,11 @@ bp_status bp_csr_plan_build(const float* data, int64_t ndata, const void* indice
                             bp_itype itype, int64_t nnz, int64_t m, int64_t n, int32_t tile_w, void* mem,
                             size_t bytes, bp_csr_plan* plan_out, bp_stream_t stream);
 
-/* device arrays inside a plan (row_start[m], tile_off[m][n_tiles+1], idx[entries], w or NULL) */
-bp_status bp_csr_plan_arrays(const bp_csr_plan* plan, const uint64_t** row_start, const uint32_t** tile_off,
-                             const uint16_t** idx, const float** w);
+/* device arrays inside a plan: seg_off[m][n_tiles+1] (segment t of row r is the 16-byte chunks
+ * [seg_off[r][t], seg_off[r][t+1]) of idx, 8 tile-local indices each, 0xFFFF padding),
+ * idx[entries], w[entries] or NULL */
+bp_status bp_csr_plan_arrays(const bp_csr_plan* plan, const uint32_t** seg_off, const uint16_t** idx,
+                             const float** w);
 
 /* event.csrmv, transpose=1, on a plan: out (n) = sum of the active rows.  `w_homo` is the
  * homogeneous weight (device pointer to one float) for homogeneous plans and is ignored for
@@ -234,8 +237,7 @@ bp_status bp_lif_coba_step_dev(const bp_lif_params* params, int64_t n, float* V,
 typedef struct {
   int32_t n, n_exc;
   int32_t tile_w, n_tiles;
-  const uint64_t* row_start; /* plan arrays of the network's CSR (bp_csr_plan, homogeneous) */
-  const uint32_t* tile_off;
+  const uint32_t* seg_off;   /* plan arrays of the network's CSR (bp_csr_plan, homogeneous) */
   const uint16_t* idx;
   float we, wi;
   bp_lif_params p;

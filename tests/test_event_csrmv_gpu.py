@@ -211,3 +211,18 @@ def test_plan_cache_and_rowpar_agree(ev, orc, monkeypatch):
   n_before = len(ev._PLANS)
   ev.csrmv(0.5, ind, ptr, events, shape=(n, n), transpose=True)
   assert len(ev._PLANS) == n_before + 1 or len(ev._PLANS) >= 1
+
+
+@pytest.mark.parametrize("variant", ["1,1,0", "2,1,1", "4,1,0", "2,2,1", "8,1,1", "8,2,0"])
+def test_tiled_kernel_variants(bplib, orc, variant):
+  """The planned kernels in every compiled variant (lanes per segment, chunk rounds, L2
+  prefetch), on rows of uneven length including one far longer than a round.  Runs in a
+  child process (the variant is read once per process)."""
+  import os
+  import subprocess
+  import sys
+  env = dict(os.environ, BPGPU_TILED=variant)
+  here = os.path.dirname(os.path.abspath(__file__))
+  r = subprocess.run([sys.executable, os.path.join(here, "_tiled_case.py")], env=env, capture_output=True, text=True,
+                     timeout=600)
+  assert r.returncode == 0 and r.stdout.strip().endswith("OK"), r.stdout[-2000:] + r.stderr[-4000:]

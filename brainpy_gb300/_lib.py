@@ -123,8 +123,24 @@ def check(status, what):
   raise BPError(full)
 
 
+_RAW_STREAM = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+
+
+def raw_stream(device=None):
+  """cudaStream_t (as an int) of the current stream on `device`."""
+  if _RAW_STREAM is not None:
+    if device is None:
+      idx = torch.cuda.current_device()
+    elif isinstance(device, torch.device):
+      idx = device.index if device.index is not None else torch.cuda.current_device()
+    else:
+      idx = int(device)
+    return _RAW_STREAM(idx)
+  return torch.cuda.current_stream(device).cuda_stream
+
+
 def stream_handle(device=None):
-  return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+  return ctypes.c_void_p(raw_stream(device))
 
 
 def ptr(t):

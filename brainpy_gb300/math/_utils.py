@@ -13,6 +13,9 @@ def default_device():
 
 def as_tensor(x, device=None, dtype=None):
   """Returns `x` as a tensor on the CUDA device (host arrays are copied)."""
+  if (dtype is None and isinstance(x, torch.Tensor) and x.is_cuda and device is not None
+      and x.device.index == device.index and x.is_contiguous()):
+    return x  # already a contiguous tensor on the device
   if device is None:
     device = default_device()
   if isinstance(x, torch.Tensor):
@@ -28,10 +31,22 @@ def as_tensor(x, device=None, dtype=None):
   return t.contiguous()
 
 
+_SCALARS = {}
+
+
 def float_data(data, device):
-  """`data` as a 1-D float32 tensor (BrainPy's jnp.atleast_1d(data))."""
+  """`data` as a 1-D float32 tensor (BrainPy's jnp.atleast_1d(data)).  Python scalars are
+  kept as one cached device tensor per (device, value), so a call with a scalar weight does
+  not copy it to the device every time."""
   if isinstance(data, (float, int)) and not isinstance(data, bool):
-    return torch.tensor([float(data)], dtype=torch.float32, device=device)
+    key = (device, float(data))
+    t = _SCALARS.get(key)
+    if t is None:
+      if len(_SCALARS) >= 256:
+        _SCALARS.clear()
+      t = torch.tensor([float(data)], dtype=torch.float32, device=device)
+      _SCALARS[key] = t
+    return t
   t = as_tensor(data, device)
   if t.ndim == 0:
     t = t.reshape(1)

@@ -49,25 +49,37 @@ class CSRPlan:
     _lib.check(st, "csr_plan_build")
     self.heter = bool(heter)
     self.device = dev
+    # per-call state kept ready: the C plan struct, a unit weight, and one workspace per stream
+    # (calls on one stream are ordered, so they can share it)
+    self._L = L
+    self._cref = ctypes.byref(self.c)
+    self._one = torch.ones(1, dtype=torch.float32, device=dev)
+    self._ws_bytes = L.bp_event_csrmv_planned_workspace_size(self._cref)
+    self._ws = {}
+
+  def _workspace(self, stream_ptr):
+    ws = self._ws.get(stream_ptr)
+    if ws is None:
+      ws = torch.empty(max(self._ws_bytes, 1), dtype=torch.uint8, device=self.device)
+      self._ws[stream_ptr] = ws
+    return ws
 
   def csrmv(self, events, data=None, out=None, float_rule=_lib.BP_EV_F32_POS):
     """out (n) = event-driven transpose product on this plan."""
-    dev = self.device
     etype, ev = event_type(events, float_rule)
     m, n = self.shape
     if ev.shape[0] != m:
       raise ValueError(f"Shape mismatch, vec ({ev.shape[0]},) @ mat {self.shape}.")
     if out is None:
-      out = torch.empty(n, dtype=torch.float32, device=dev)
-    L = _lib.lib()
-    w = None
+      out = torch.empty(n, dtype=torch.float32, device=self.device)
+    w = 0
     if not self.heter:
-      w = data if data is not None else torch.ones(1, dtype=torch.float32, device=dev)
-    ws_bytes = L.bp_event_csrmv_planned_workspace_size(ctypes.byref(self.c))
-    ws = _lib.workspace(ws_bytes, dev)
-    st = L.bp_event_csrmv_planned(ctypes.byref(self.c), _lib.ptr(w) if w is not None else None, _lib.ptr(ev), etype,
-                                  _lib.ptr(out), self.cluster, _lib.ptr(ws), ws_bytes, _lib.stream_handle(dev))
-    _lib.check(st, "event_csrmv_planned")
+      w = (data if data is not None else self._one).data_ptr()
+    sp = _lib.raw_stream(self.device)
+    st = self._L.bp_event_csrmv_planned(self._cref, w, ev.data_ptr(), etype, out.data_ptr(), self.cluster,
+                                        self._workspace(sp).data_ptr(), self._ws_bytes, sp)
+    if st:
+      _lib.check(st, "event_csrmv_planned")
     return out
 
 
@@ -79,15 +91,14 @@ class CSRPlan:
       raise ValueError(f"Shape mismatch, vec ({vector.shape[0]},) @ mat {self.shape}.")
     if out is None:
       out = torch.empty(n, dtype=torch.float32, device=dev)
-    L = _lib.lib()
-    w = None
+    w = 0
     if not self.heter:
-      w = data if data is not None else torch.ones(1, dtype=torch.float32, device=dev)
-    ws_bytes = L.bp_event_csrmv_planned_workspace_size(ctypes.byref(self.c))
-    ws = _lib.workspace(ws_bytes, dev)
-    st = L.bp_csrmv_planned(ctypes.byref(self.c), _lib.ptr(w) if w is not None else None, _lib.ptr(vector),
-                            _lib.ptr(out), self.cluster, _lib.ptr(ws), ws_bytes, _lib.stream_handle(dev))
-    _lib.check(st, "csrmv_planned")
+      w = (data if data is not None else self._one).data_ptr()
+    sp = _lib.raw_stream(dev)
+    st = self._L.bp_csrmv_planned(self._cref, w, vector.data_ptr(), out.data_ptr(), self.cluster,
+                                  self._workspace(sp).data_ptr(), self._ws_bytes, sp)
+    if st:
+      _lib.check(st, "csrmv_planned")
     return out
 
 

@@ -43,10 +43,11 @@ def parse():
   ap.add_argument("--no-cpu-baseline", action="store_true")
   ap.add_argument("--cpu-seconds", type=float, default=12.0)
   ap.add_argument("--workload", default="event_csrmv",
-                  choices=["event_csrmv", "coba", "batched", "jitconn_net", "serve"],
+                  choices=["event_csrmv", "coba", "batched", "jitconn_net", "serve", "sweep"],
                   help="event_csrmv (headline); coba: the 4000-neuron COBA example; batched: 256 uneven "
                        "networks in persistent cluster launches vs the plain per-network path; jitconn_net: "
-                       "4M-neuron just-in-time network; serve: continuous-batching serving loop")
+                       "4M-neuron just-in-time network; serve: continuous-batching serving loop; sweep: the "
+                       "operator sweep (event/sparse csrmv, jitconn) as one JSON line")
   ap.add_argument("--nets", type=int, default=256)
   ap.add_argument("--sim-steps", type=int, default=0, help="override the workload's number of steps")
   return ap.parse_args()
@@ -188,7 +189,8 @@ def run_reference(args):
 def main():
   args = parse()
   if args.workload != "event_csrmv":
-    fn = {"coba": bench_coba, "batched": bench_batched, "jitconn_net": bench_jitconn_net, "serve": bench_serve}
+    fn = {"coba": bench_coba, "batched": bench_batched, "jitconn_net": bench_jitconn_net, "serve": bench_serve,
+          "sweep": bench_sweep}
     line = fn[args.workload](args)
     if line is not None:
       print(json.dumps(line))
@@ -474,6 +476,80 @@ def bench_jitconn_net(args):
 def bench_serve(args):
   from brainpy_gb300 import serve
   return serve.bench(args)
+
+
+def _graph_time(fn, flush_buf, steps=20):
+  """Mean device time of one CUDA-graph replay of fn(), L2 flushed before each replay."""
+  side = torch.cuda.Stream()
+  side.wait_stream(torch.cuda.current_stream())
+  with torch.cuda.stream(side):
+    fn()
+  torch.cuda.current_stream().wait_stream(side)
+  torch.cuda.synchronize()
+  g = torch.cuda.CUDAGraph()
+  with torch.cuda.graph(g):
+    fn()
+  for _ in range(3):
+    flush_buf.zero_()
+    g.replay()
+  torch.cuda.synchronize()
+  ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+  for a, b in ev:
+    flush_buf.zero_()
+    a.record()
+    g.replay()
+    b.record()
+  torch.cuda.synchronize()
+  return sum(a.elapsed_time(b) for a, b in ev) / steps * 1e-3
+
+
+def bench_sweep(args):
+  """The operator sweep: event.csrmv transpose=True on square FixedProb CSR, N in {1e4, 1e5,
+  1e6}, K in {100, 1000}, rate in {0.5, 2, 10} %, homogeneous 1.0 / heterogeneous N(0.5, 0.1);
+  sparse.csrmv transpose=True on a dense N(0, 1) vector; jitconn event_mv_prob_{homo, uniform,
+  normal} with p = K/N, seed 42, both outdim_parallel.  One JSON line with every point."""
+  from brainpy_gb300.connect import bernoulli_events, fixed_prob_csr, normal_weights
+  from brainpy_gb300.math import event, jitconn, sparse
+  peak, _ = load_peaks()
+  flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+  pts = []
+  for n in (10_000, 100_000, 1_000_000):
+    for k in (100, 1000):
+      ind, ptr = fixed_prob_csr(n, n, k, seed=0)
+      wh = normal_weights(ind.numel(), 0.5, 0.1, seed=1)
+      one = torch.ones(1, device="cuda")
+      for rate in (0.005, 0.02, 0.1):
+        sp = bernoulli_events(n, rate, seed=2)
+        a = int(sp.sum())
+        for name, data in (("homo", one), ("heter", wh)):
+          t = _graph_time(lambda: event.csrmv(data, ind, ptr, sp, shape=(n, n), transpose=True), flush_buf)
+          b = alg_bytes(n, a, k, name == "heter")
+          pts.append({"op": "event.csrmv", "T": True, "n": n, "k": k, "rate": rate, "w": name, "us": t * 1e6,
+                      "events_per_s": a * k / t, "hbm_frac": b / t / 1e9 / peak})
+      x = torch.randn(n, device="cuda")
+      t = _graph_time(lambda: sparse.csrmv(one, ind, ptr, x, shape=(n, n), transpose=True), flush_buf)
+      b = 4 * (n + 1) + 4 * ind.numel() + 8 * n
+      pts.append({"op": "sparse.csrmv", "T": True, "n": n, "k": k, "w": "homo", "us": t * 1e6,
+                  "nnz_per_s": ind.numel() / t, "hbm_frac": b / t / 1e9 / peak})
+      del ind, ptr, wh
+      torch.cuda.empty_cache()
+      sp = bernoulli_events(n, 0.02, seed=2)
+      for fn, kw in ((jitconn.event_mv_prob_homo, dict(weight=1.0)),
+                     (jitconn.event_mv_prob_uniform, dict(w_low=0.0, w_high=1.0)),
+                     (jitconn.event_mv_prob_normal, dict(w_mu=0.0, w_sigma=1.0))):
+        for odp in (True, False):
+          t = _graph_time(lambda: fn(sp, conn_prob=k / n, seed=42, shape=(n, n), outdim_parallel=odp, **kw),
+                          flush_buf)
+          pts.append({"op": fn.__name__, "n": n, "k": k, "rate": 0.02, "outdim_parallel": odp, "us": t * 1e6,
+                      "connections_per_s": n * k / t})
+  head = [p_ for p_ in pts if p_["op"] == "event.csrmv" and p_["n"] == 1_000_000 and p_["k"] == 1000
+          and p_["rate"] == 0.02 and p_["w"] == "homo"][0]
+  return {"metric": "operator sweep (event/sparse csrmv transpose, jitconn)", "value": head["events_per_s"],
+          "unit": "events/s", "n_gpus": 1, "steps": 20, "warmup": 3, "ms_per_step": head["us"] * 1e-3,
+          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+          "config": {"workload": "operator sweep; value = event.csrmv T N=1e6 K=1000 r=2% homo",
+                     "l2": "flushed before each replay", "timing": "CUDA-graph replay, CUDA events"},
+          "points": pts}
 
 
 def launches_per_step(args):

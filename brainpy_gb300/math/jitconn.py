@@ -121,12 +121,15 @@ def _make(kind, event, taichi):
            transpose: bool = False, outdim_parallel: bool = True, variant: str = "gpu"):
       return _mv(kind, event, vector, _scalar(weight, "weight"), 0.0, conn_prob, seed, shape, transpose,
                  outdim_parallel, taichi, variant)
-  else:
-    names = ("w_low", "w_high") if kind == "uniform" else ("w_mu", "w_sigma")
-
-    def op(vector, w_a, w_b, conn_prob, seed: Optional[int] = None, *, shape: Tuple[int, int],
+  elif kind == "uniform":
+    def op(vector, w_low, w_high, conn_prob, seed: Optional[int] = None, *, shape: Tuple[int, int],
            transpose: bool = False, outdim_parallel: bool = True, variant: str = "gpu"):
-      return _mv(kind, event, vector, _scalar(w_a, names[0]), _scalar(w_b, names[1]), conn_prob, seed, shape,
+      return _mv(kind, event, vector, _scalar(w_low, "w_low"), _scalar(w_high, "w_high"), conn_prob, seed, shape,
+                 transpose, outdim_parallel, taichi, variant)
+  else:
+    def op(vector, w_mu, w_sigma, conn_prob, seed: Optional[int] = None, *, shape: Tuple[int, int],
+           transpose: bool = False, outdim_parallel: bool = True, variant: str = "gpu"):
+      return _mv(kind, event, vector, _scalar(w_mu, "w_mu"), _scalar(w_sigma, "w_sigma"), conn_prob, seed, shape,
                  transpose, outdim_parallel, taichi, variant)
   op.__name__ = f"{'event_' if event else ''}mv_prob_{kind}{'_taichi' if taichi else ''}"
   op.__doc__ = _doc(kind, event) + (" Taichi twin: conn_len from a double-precision 1/conn_prob." if taichi else "")

@@ -146,19 +146,31 @@ __global__ void __launch_bounds__(256) compact_blocked_kernel(const void* __rest
 //   kWRow   heterogeneous weights, dense vector x: float32 sum of w_ij * x_i
 enum { kCount = 0, kWeight = 1, kRowVal = 2, kWRow = 3 };
 
+// Shared-memory reductions issued under a predicate (no branch): entries with index >= lim
+// are skipped -- the 0xFFFF padding, and every entry of a chunk given lim = 0.
+__device__ __forceinline__ void red_if(uint32_t x, uint32_t lim, uint32_t addr, uint32_t v) {
+  asm volatile("{\n\t.reg .pred p;\n\tsetp.lt.u32 p, %0, %1;\n\t@p red.shared.add.u32 [%2], %3;\n\t}" ::"r"(x),
+               "r"(lim), "r"(addr), "r"(v));
+}
+__device__ __forceinline__ void red_if(uint32_t x, uint32_t lim, uint32_t addr, float v) {
+  asm volatile("{\n\t.reg .pred p;\n\tsetp.lt.u32 p, %0, %1;\n\t@p red.shared.add.f32 [%2], %3;\n\t}" ::"r"(x),
+               "r"(lim), "r"(addr), "f"(v));
+}
+
+// Adds the 8 entries of one chunk (tile-local indices) into the accumulator at shared-memory
+// address acc_s.
 template <int MODE>
-__device__ __forceinline__ void accumulate8(uint32_t* acc, uint4 v, float4 w0, float4 w1, float xv, uint32_t tile_w) {
+__device__ __forceinline__ void accumulate8(uint32_t acc_s, uint4 v, float4 w0, float4 w1, float xv, uint32_t lim) {
   const uint32_t x[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
                          v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
   const float ww[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
-    if (x[q] < tile_w) {  // excludes the 0xFFFF padding
-      if (MODE == kCount) atomicAdd(acc + x[q], 1u);
-      else if (MODE == kWeight) atomicAdd(reinterpret_cast<float*>(acc) + x[q], ww[q]);
-      else if (MODE == kRowVal) atomicAdd(reinterpret_cast<float*>(acc) + x[q], xv);
-      else atomicAdd(reinterpret_cast<float*>(acc) + x[q], __fmul_rn(ww[q], xv));
-    }
+    const uint32_t ad = acc_s + 4u * x[q];
+    if (MODE == kCount) red_if(x[q], lim, ad, 1u);
+    else if (MODE == kWeight) red_if(x[q], lim, ad, ww[q]);
+    else if (MODE == kRowVal) red_if(x[q], lim, ad, xv);
+    else red_if(x[q], lim, ad, __fmul_rn(ww[q], xv));
   }
 }
 
@@ -197,6 +209,8 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const Ti
   constexpr unsigned FULL = 0xffffffffu;
   extern __shared__ __align__(16) unsigned char smem[];
   uint32_t* acc = reinterpret_cast<uint32_t*>(smem);
+  const uint32_t acc_s = (uint32_t)__cvta_generic_to_shared(acc);
+  const uint32_t tile_w = (uint32_t)a.tile_w;
   int* s_boff = reinterpret_cast<int*>(smem + sizeof(uint32_t) * (size_t)a.acc_words);  // kBlockGroup + 1
   __shared__ int s_wsum[32];
 
@@ -305,7 +319,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const Ti
         for (int u0 = 0; u0 < G; u0 += UB) {
           uint4 vv[UB][RND];
           float4 w0[UB][RND], w1[UB][RND];
-          uint32_t st[UB], ln[UB];
+          uint32_t st[UB], ln[UB], lim[UB][RND];
           float xs[UB];
 #pragma unroll
           for (int u = 0; u < UB; ++u) {
@@ -315,14 +329,16 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const Ti
             xs[u] = HAS_X ? __shfl_sync(FULL, cxv, j) : 0.0f;
 #pragma unroll
             for (int r = 0; r < RND; ++r) {
+              // every lane loads a chunk of its segment (chunk 0, or the chunk where the empty
+              // segment would start, past the end); lanes past the end add nothing (lim = 0)
               const uint32_t c = gl + r * G;
-              if (c < ln[u]) {
-                const uint64_t e = 8ull * (st[u] + c);
-                vv[u][r] = ld_stream_u4(a.idx + e);
-                if (HAS_W) {
-                  w0[u][r] = ld_stream_f4(a.w + e);
-                  w1[u][r] = ld_stream_f4(a.w + e + 4);
-                }
+              const bool in = c < ln[u];
+              lim[u][r] = in ? tile_w : 0u;
+              const uint64_t e = 8ull * (st[u] + (in ? c : 0u));
+              vv[u][r] = ld_stream_u4(a.idx + e);
+              if (HAS_W) {
+                w0[u][r] = ld_stream_f4(a.w + e);
+                w1[u][r] = ld_stream_f4(a.w + e + 4);
               }
             }
           }
@@ -330,9 +346,8 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const Ti
           for (int u = 0; u < UB; ++u)
 #pragma unroll
             for (int r = 0; r < RND; ++r)
-              if (gl + r * G < ln[u])
-                accumulate8<MODE>(acc, vv[u][r], HAS_W ? w0[u][r] : make_float4(0, 0, 0, 0),
-                                  HAS_W ? w1[u][r] : make_float4(0, 0, 0, 0), xs[u], (uint32_t)a.tile_w);
+              accumulate8<MODE>(acc_s, vv[u][r], HAS_W ? w0[u][r] : make_float4(0, 0, 0, 0),
+                                HAS_W ? w1[u][r] : make_float4(0, 0, 0, 0), xs[u], lim[u][r]);
           // chunks beyond RND*G (long segments)
 #pragma unroll
           for (int u = 0; u < UB; ++u) {
@@ -344,7 +359,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const Ti
                 y0 = ld_stream_f4(a.w + e);
                 y1 = ld_stream_f4(a.w + e + 4);
               }
-              accumulate8<MODE>(acc, x, y0, y1, xs[u], (uint32_t)a.tile_w);
+              accumulate8<MODE>(acc_s, x, y0, y1, xs[u], tile_w);
             }
           }
         }

@@ -1,0 +1,168 @@
+"""The synaptic-projection layers that call the propagation operators, as in
+brainpy/_src/dnn/linear.py: CSRLinear / EventCSRLinear (:490-649) and
+JitFP{Homo,Uniform,Normal}Linear / EventJitFP{Homo,Uniform,Normal}Linear (:805-1280).
+
+Same constructor arguments and `update` semantics: CSR layers take the connection's
+(indices, indptr) -- from `conn.require('csr')` when given a BrainPy-style connector -- with
+shape (pre_num, post_num) and transpose=True by default; just-in-time layers use
+shape=(num_out, num_in) and outdim_parallel = not atomic.  Inputs of more than one dimension
+are treated as a batch of vectors along the last axis.  Training modes, sharding and
+synaptic plasticity are not part of this package.
+"""
+from typing import Optional
+
+import numpy as np
+import torch
+
+from .math import event as _event
+from .math import jitconn as _jitconn
+from .math import sparse as _sparse
+from .math._utils import as_tensor, default_device
+
+__all__ = ["CSRLinear", "EventCSRLinear", "JitFPHomoLinear", "JitFPUniformLinear", "JitFPNormalLinear",
+           "EventJitFPHomoLinear", "EventJitFPUniformLinear", "EventJitFPNormalLinear"]
+
+
+def _batched(fn, x):
+  """fn over the last axis of x (fn takes and returns 1-D tensors)."""
+  if x.ndim == 1:
+    return fn(x)
+  if x.ndim == 0:
+    raise ValueError("the input must have at least one dimension")
+  lead = x.shape[:-1]
+  flat = x.reshape(-1, x.shape[-1])
+  ys = [fn(flat[b]) for b in range(flat.shape[0])]
+  y = torch.stack(ys) if ys else torch.empty((0, 0), dtype=torch.float32, device=x.device)
+  return y.reshape(tuple(lead) + (y.shape[-1],))
+
+
+class _CSRLayer:
+  """A fixed CSR connection with a scalar or per-synapse weight (linear.py:490-527)."""
+
+  def __init__(self, conn, weight, transpose: bool = True, shape=None, name: Optional[str] = None):
+    if hasattr(conn, "require"):
+      indices, indptr = conn.require("csr")
+      pre_num, post_num = int(conn.pre_num), int(conn.post_num)
+    else:
+      indices, indptr = conn
+      if shape is None:
+        raise ValueError("shape=(pre_num, post_num) is required when the connection is given as (indices, indptr)")
+      pre_num, post_num = int(shape[0]), int(shape[1])
+    dev = default_device()
+    self.indices = as_tensor(indices, dev)
+    self.indptr = as_tensor(indptr, dev)
+    if self.indptr.numel() != pre_num + 1:
+      raise ValueError(f"indptr should have {pre_num + 1} entries, got {self.indptr.numel()}")
+    self.pre_num, self.post_num = pre_num, post_num
+    self.transpose = bool(transpose)
+    if isinstance(weight, (float, int)) and not isinstance(weight, bool):
+      self.weight = float(weight)
+    else:
+      w = as_tensor(np.asarray(weight, np.float32) if not isinstance(weight, torch.Tensor) else weight, dev)
+      if w.numel() not in (1, self.indices.numel()):
+        raise ValueError(f"weight should be a scalar or have {self.indices.numel()} entries, got {w.numel()}")
+      self.weight = w.reshape(-1).to(torch.float32)
+    self.name = name
+
+  def __call__(self, x):
+    return self.update(x)
+
+
+class CSRLinear(_CSRLayer):
+  """y = x @ W (transpose=True) or W @ x with W a CSR matrix; sparse.csrmv (linear.py:555-609)."""
+
+  def __init__(self, conn, weight, method: str = "cusparse", transpose: bool = True, shape=None,
+               name: Optional[str] = None):
+    super().__init__(conn, weight, transpose=transpose, shape=shape, name=name)
+    self.method = method
+
+  def update(self, x):
+    x = as_tensor(x, default_device())
+    return _batched(lambda v: _sparse.csrmv(self.weight, self.indices, self.indptr, v,
+                                            shape=(self.pre_num, self.post_num), transpose=self.transpose,
+                                            method=self.method), x)
+
+
+class EventCSRLinear(_CSRLayer):
+  """Event-driven y = spikes @ W on a CSR matrix; event.csrmv (linear.py:600-649)."""
+
+  def update(self, x):
+    x = as_tensor(x, default_device())
+    return _batched(lambda v: _event.csrmv(self.weight, self.indices, self.indptr, v,
+                                           shape=(self.pre_num, self.post_num), transpose=self.transpose), x)
+
+
+class _JitLayer:
+  """A just-in-time connection of probability `prob` between num_in inputs and num_out outputs
+  (linear.py:805-1280): the seed is drawn once when not given."""
+
+  def __init__(self, num_in: int, num_out: int, prob: float, seed: Optional[int] = None, transpose: bool = False,
+               atomic: bool = False, name: Optional[str] = None):
+    self.num_in, self.num_out = int(num_in), int(num_out)
+    self.prob = float(prob)
+    self.seed = int(np.random.randint(0, 1000000)) if seed is None else int(seed)
+    self.transpose = bool(transpose)
+    self.atomic = bool(atomic)
+    self.name = name
+
+  def _call(self, op, x, *weights):
+    x = as_tensor(x, default_device())
+    return _batched(lambda v: op(v, *weights, self.prob, self.seed, shape=(self.num_out, self.num_in),
+                                 transpose=self.transpose, outdim_parallel=not self.atomic), x)
+
+  def __call__(self, x):
+    return self.update(x)
+
+
+class JitFPHomoLinear(_JitLayer):
+  """y = M x, M ~ Bernoulli(prob) with one weight; jitconn.mv_prob_homo."""
+
+  def __init__(self, num_in, num_out, prob, weight, seed=None, transpose=False, atomic=False, name=None):
+    super().__init__(num_in, num_out, prob, seed, transpose, atomic, name)
+    self.weight = float(weight)
+
+  def update(self, x):
+    return self._call(_jitconn.mv_prob_homo, x, self.weight)
+
+
+class JitFPUniformLinear(_JitLayer):
+  """y = M x, M ~ Bernoulli(prob) with U[w_low, w_high] weights; jitconn.mv_prob_uniform."""
+
+  def __init__(self, num_in, num_out, prob, w_low, w_high, seed=None, transpose=False, atomic=False, name=None):
+    super().__init__(num_in, num_out, prob, seed, transpose, atomic, name)
+    self.w_low, self.w_high = float(w_low), float(w_high)
+
+  def update(self, x):
+    return self._call(_jitconn.mv_prob_uniform, x, self.w_low, self.w_high)
+
+
+class JitFPNormalLinear(_JitLayer):
+  """y = M x, M ~ Bernoulli(prob) with N(w_mu, w_sigma) weights; jitconn.mv_prob_normal."""
+
+  def __init__(self, num_in, num_out, prob, w_mu, w_sigma, seed=None, transpose=False, atomic=False, name=None):
+    super().__init__(num_in, num_out, prob, seed, transpose, atomic, name)
+    self.w_mu, self.w_sigma = float(w_mu), float(w_sigma)
+
+  def update(self, x):
+    return self._call(_jitconn.mv_prob_normal, x, self.w_mu, self.w_sigma)
+
+
+class EventJitFPHomoLinear(JitFPHomoLinear):
+  """Event-driven JitFPHomoLinear; jitconn.event_mv_prob_homo (linear.py:1044-1120)."""
+
+  def update(self, x):
+    return self._call(_jitconn.event_mv_prob_homo, x, self.weight)
+
+
+class EventJitFPUniformLinear(JitFPUniformLinear):
+  """Event-driven JitFPUniformLinear; jitconn.event_mv_prob_uniform (linear.py:1123-1200)."""
+
+  def update(self, x):
+    return self._call(_jitconn.event_mv_prob_uniform, x, self.w_low, self.w_high)
+
+
+class EventJitFPNormalLinear(JitFPNormalLinear):
+  """Event-driven JitFPNormalLinear; jitconn.event_mv_prob_normal (linear.py:1203-1280)."""
+
+  def update(self, x):
+    return self._call(_jitconn.event_mv_prob_normal, x, self.w_mu, self.w_sigma)

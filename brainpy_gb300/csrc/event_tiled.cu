@@ -297,6 +297,67 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const Ti
     fetch_desc(fetch_row(k, blk), cst, cn, cxv);                 // slice k
     fetch_desc(fetch_row(k + nwarps, blk), nst, nn, nxv);        // slice k + W
     int32_t row2 = fetch_row(k + 2 * nwarps, blk);               // slice k + 2W
+
+    // A unit is UB rounds of a slice: in round u, lane group grp takes segment grp + u * NG and
+    // lane gl loads its chunks gl, gl + G, ... (RND of them), 8 tile-local indices each.
+    constexpr int NG = 32 / G;
+    constexpr int UBMAX = (HAS_W ? 1 : 2) / RND > 0 ? (HAS_W ? 1 : 2) / RND : 1;
+    constexpr int UB = UBMAX > G ? G : UBMAX;
+    constexpr int NU = G / UB;  // units per slice
+    const int grp = lane / G, gl = lane % G;
+    struct Unit {
+      uint4 vv[UB][RND];
+      float4 w0[UB][RND], w1[UB][RND];
+      uint32_t st[UB], ln[UB], lim[UB][RND];
+      float xs[UB];
+    };
+    auto load_unit = [&](Unit& U, uint32_t sst, uint32_t sn, float sxv, int u0) {
+#pragma unroll
+      for (int u = 0; u < UB; ++u) {
+        const int j = grp + (u0 + u) * NG;
+        U.st[u] = __shfl_sync(FULL, sst, j);
+        U.ln[u] = __shfl_sync(FULL, sn, j);
+        U.xs[u] = HAS_X ? __shfl_sync(FULL, sxv, j) : 0.0f;
+#pragma unroll
+        for (int r = 0; r < RND; ++r) {
+          // every lane loads a chunk of its segment (chunk 0, or the chunk where the empty
+          // segment would start, past the end); lanes past the end add nothing (lim = 0)
+          const uint32_t c = gl + r * G;
+          const bool in = c < U.ln[u];
+          U.lim[u][r] = in ? tile_w : 0u;
+          const uint64_t e = 8ull * (U.st[u] + (in ? c : 0u));
+          U.vv[u][r] = ld_stream_u4(a.idx + e);
+          if (HAS_W) {
+            U.w0[u][r] = ld_stream_f4(a.w + e);
+            U.w1[u][r] = ld_stream_f4(a.w + e + 4);
+          }
+        }
+      }
+    };
+    auto consume_unit = [&](const Unit& U) {
+#pragma unroll
+      for (int u = 0; u < UB; ++u)
+#pragma unroll
+        for (int r = 0; r < RND; ++r)
+          accumulate8<MODE>(acc_s, U.vv[u][r], HAS_W ? U.w0[u][r] : make_float4(0, 0, 0, 0),
+                            HAS_W ? U.w1[u][r] : make_float4(0, 0, 0, 0), U.xs[u], U.lim[u][r]);
+      // chunks beyond RND*G (long segments), loaded here
+#pragma unroll
+      for (int u = 0; u < UB; ++u) {
+        for (uint32_t c = gl + RND * G; c < U.ln[u]; c += G) {
+          const uint64_t e = 8ull * (U.st[u] + c);
+          const uint4 x = ld_stream_u4(a.idx + e);
+          float4 y0 = make_float4(0, 0, 0, 0), y1 = y0;
+          if (HAS_W) {
+            y0 = ld_stream_f4(a.w + e);
+            y1 = ld_stream_f4(a.w + e + 4);
+          }
+          accumulate8<MODE>(acc_s, x, y0, y1, U.xs[u], tile_w);
+        }
+      }
+    };
+    Unit cur, nxt;
+    load_unit(cur, cst, cn, cxv, 0);
     while (k < nslices) {
       fetch_desc(row2, mst, mn, mxv);                            // slice k + 2W
       row2 = fetch_row(k + 3 * nwarps, blk);                     // slice k + 3W
@@ -310,59 +371,14 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const Ti
           }
         }
       }
-      {
-        constexpr int NG = 32 / G;
-        constexpr int UBMAX = (HAS_W ? 2 : 4) / RND > 0 ? (HAS_W ? 2 : 4) / RND : 1;
-        constexpr int UB = UBMAX > G ? G : UBMAX;
-        const int grp = lane / G, gl = lane % G;
-#pragma unroll 1
-        for (int u0 = 0; u0 < G; u0 += UB) {
-          uint4 vv[UB][RND];
-          float4 w0[UB][RND], w1[UB][RND];
-          uint32_t st[UB], ln[UB], lim[UB][RND];
-          float xs[UB];
+      // This slice's units: the loads of the next unit (of this slice, or the first unit of
+      // slice k + W) are issued before the current unit's atomics.
 #pragma unroll
-          for (int u = 0; u < UB; ++u) {
-            const int j = grp + (u0 + u) * NG;
-            st[u] = __shfl_sync(FULL, cst, j);
-            ln[u] = __shfl_sync(FULL, cn, j);
-            xs[u] = HAS_X ? __shfl_sync(FULL, cxv, j) : 0.0f;
-#pragma unroll
-            for (int r = 0; r < RND; ++r) {
-              // every lane loads a chunk of its segment (chunk 0, or the chunk where the empty
-              // segment would start, past the end); lanes past the end add nothing (lim = 0)
-              const uint32_t c = gl + r * G;
-              const bool in = c < ln[u];
-              lim[u][r] = in ? tile_w : 0u;
-              const uint64_t e = 8ull * (st[u] + (in ? c : 0u));
-              vv[u][r] = ld_stream_u4(a.idx + e);
-              if (HAS_W) {
-                w0[u][r] = ld_stream_f4(a.w + e);
-                w1[u][r] = ld_stream_f4(a.w + e + 4);
-              }
-            }
-          }
-#pragma unroll
-          for (int u = 0; u < UB; ++u)
-#pragma unroll
-            for (int r = 0; r < RND; ++r)
-              accumulate8<MODE>(acc_s, vv[u][r], HAS_W ? w0[u][r] : make_float4(0, 0, 0, 0),
-                                HAS_W ? w1[u][r] : make_float4(0, 0, 0, 0), xs[u], lim[u][r]);
-          // chunks beyond RND*G (long segments)
-#pragma unroll
-          for (int u = 0; u < UB; ++u) {
-            for (uint32_t c = gl + RND * G; c < ln[u]; c += G) {
-              const uint64_t e = 8ull * (st[u] + c);
-              const uint4 x = ld_stream_u4(a.idx + e);
-              float4 y0 = make_float4(0, 0, 0, 0), y1 = y0;
-              if (HAS_W) {
-                y0 = ld_stream_f4(a.w + e);
-                y1 = ld_stream_f4(a.w + e + 4);
-              }
-              accumulate8<MODE>(acc_s, x, y0, y1, xs[u], tile_w);
-            }
-          }
-        }
+      for (int u = 0; u < NU; ++u) {
+        if (u + 1 < NU) load_unit(nxt, cst, cn, cxv, (u + 1) * UB);
+        else load_unit(nxt, nst, nn, nxv, 0);
+        consume_unit(cur);
+        cur = nxt;
       }
       cst = nst;
       cn = nn;

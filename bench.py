@@ -255,13 +255,9 @@ def main():
   # the graphed results equal eager calls on the same spikes
   for i in range(min(nv, args.steps)):
     assert torch.equal(outs[i], step(i)), "graph replay and eager call disagree"
-  if ws > 1:
-    t = torch.tensor([step_ms], device=device, dtype=torch.float64)
-    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    step_ms = float(t)
-    ev_t = torch.tensor([events_done], device=device, dtype=torch.float64)
-    torch.distributed.all_reduce(ev_t)
-    events_done = float(ev_t)
+  # replicas: the slowest rank's time, the events of all ranks
+  from brainpy_gb300 import replicas
+  step_ms, events_done = replicas.combine(step_ms, events_done)
   value = events_done / (step_ms * 1e-3 * args.steps)
 
   # The same call alone with L2 flushed before it (one graph per spike vector): the latency
@@ -336,6 +332,7 @@ def main():
   torch.cuda.synchronize()
   for j in range(min(nv, args.steps)):  # the results read back are the device results
     assert torch.equal(out_host[j], outs[j].cpu()), "e2e result differs from the device result"
+  e2e_ms, e2e_events = replicas.combine(e2e_ms, e2e_events)
   e2e = {"value": e2e_events / (e2e_ms * 1e-3), "unit": UNIT,
          "h2d_bytes_per_step": n + (4 if args.weights == "homo" else 0), "d2h_bytes_per_step": 4 * n}
 

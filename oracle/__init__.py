@@ -60,6 +60,7 @@ def lib():
         "orc_coba_net_run": (None, [_P, _I64, _I64, _P, _P, _F32, _P, _P, _F32, _P, _P, _P, _P, _P, _I32, _I32,
                                     _F32, _I32, _P, _I32, _P]),
         "cpu_event_csrmv_bool": (None, [_P, _I64, _P, _P, _P, _I64, _I64, _I32, _P]),
+        "cpu_event_csrmv_bool_t_batch": (_I32, [_P, _I64, _P, _P, _P, _I64, _I64, _I64, _P]),
         "cpu_num_threads": (_I32, []),
         "orc_bp_expf": (_F32, [_F32]),
         "orc_bp_exprel": (_F32, [_F32]),
@@ -208,6 +209,20 @@ def cpu_event_csrmv_bool(data, indices, indptr, events, shape, transpose, out=No
   lib().cpu_event_csrmv_bool(_p(data), data.shape[0], _p(indices), _p(indptr), _p(events.view(np.uint8)), m, n,
                              int(transpose), _p(out))
   return out
+
+
+def cpu_event_csrmv_bool_t_batch(data, indices, indptr, events_batch, shape, out=None):
+  """Independent transpose calls of the restated reference loop, one per host thread;
+  returns (out (nb, n), threads used)."""
+  data = np.ascontiguousarray(np.atleast_1d(data).astype(np.float32))
+  m, n = shape
+  ev = np.ascontiguousarray(events_batch).view(np.uint8)
+  nb = ev.shape[0]
+  if out is None:
+    out = np.zeros((nb, n), np.float32)
+  used = lib().cpu_event_csrmv_bool_t_batch(_p(data), data.shape[0], _p(indices), _p(indptr), _p(ev), nb, m, n,
+                                            _p(out))
+  return out, used
 
 
 def cpu_num_threads():

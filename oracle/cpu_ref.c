@@ -57,6 +57,23 @@ void cpu_event_csrmv_bool(const float* data, int64_t ndata, const int32_t* indic
   }
 }
 
+/* Independent calls of the serial transpose loop (bool events), one per thread: the
+ * reference's per-call path run concurrently on every host core, e.g. several simulations or
+ * trials at once.  events: nb vectors of m; out: nb vectors of n.  Returns the threads used. */
+int32_t cpu_event_csrmv_bool_t_batch(const float* data, int64_t ndata, const int32_t* indices,
+                                     const int32_t* indptr, const uint8_t* events, int64_t nb, int64_t m,
+                                     int64_t n, float* out) {
+  int32_t used = 1;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t b = 0; b < nb; ++b) {
+#ifdef _OPENMP
+    if (b == 0) used = (int32_t)omp_get_num_threads();
+#endif
+    cpu_event_csrmv_bool(data, ndata, indices, indptr, events + b * m, m, n, 1, out + b * n);
+  }
+  return used;
+}
+
 int32_t cpu_num_threads(void) {
 #ifdef _OPENMP
   return (int32_t)omp_get_max_threads();

@@ -107,6 +107,9 @@ void orc_coba_net_run(const orc_lif_params* p, int64_t n, int64_t n_exc,
 void cpu_event_csrmv_bool(const float* data, int64_t ndata, const int32_t* indices,
                           const int32_t* indptr, const uint8_t* events, int64_t m, int64_t n,
                           int32_t transpose, float* out);
+int32_t cpu_event_csrmv_bool_t_batch(const float* data, int64_t ndata, const int32_t* indices,
+                                     const int32_t* indptr, const uint8_t* events, int64_t nb, int64_t m,
+                                     int64_t n, float* out);
 int32_t cpu_num_threads(void);
 
 float orc_bp_expf(float x);

@@ -392,8 +392,11 @@ def bench_coba(args):
   steps = args.sim_steps or 10000
   V0 = np.random.default_rng(3).normal(-55.0, 5.0, 4000).astype(np.float32)
   net = dyn.EINetwork.fixed_prob(3200, 800, prob=0.02, seed=0, V0=V0)
-  net.run(100)  # warm-up: plan build, module load
-  net2 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=V0)
+  tile = int(os.environ.get("BPGPU_NET_TILE", "0")) or None
+  net2 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=V0, net_tile=tile)
+  net2.run(100)  # warm-up: plan build, module load
+  net2 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=V0, net_tile=tile)
+  net2._cluster_plan()  # plan built outside the timed region
   clocks = ClockSampler(torch.cuda.current_device())
   counts = torch.zeros(steps, dtype=torch.int32, device="cuda")
   t_cluster, _ = _cuda_time(lambda: net2.run(steps, spike_counts=counts))
@@ -459,7 +462,8 @@ def bench_batched(args):
     ne = int(0.8 * n)
     nets.append(dyn.EINetwork.fixed_prob(ne, n - ne, prob=0.02, we=float(rng.uniform(0.3, 1.0)),
                                          wi=float(rng.uniform(3.0, 10.0)), seed=100 + k,
-                                         V0=rng.normal(-55.0, 5.0, n).astype(np.float32)))
+                                         V0=rng.normal(-55.0, 5.0, n).astype(np.float32),
+                                         net_tile=int(os.environ.get("BPGPU_NET_TILE", "0")) or None))
   init = [(x.V.clone(), x.ge.clone(), x.gi.clone(), x.t_last.clone(), x.spike.clone()) for x in nets]
   for x in nets:
     x._cluster_plan()

@@ -57,6 +57,15 @@ def lif_coba_step(params: LifParams, V, ge, gi, t_last, spike, dge, dgi, step: i
   _lib.check(st, "lif_coba_step")
 
 
+def default_net_tile(n):
+  """Neurons per CTA of the cluster runner for an n-neuron network: a quarter of the network
+  (more CTAs per network shorten a step: measured 231 K steps/s for the 4000-neuron COBA
+  example at 1024 against 108 K at 4096), between 1024 and the runner's maximum width."""
+  cap = _lib.lib().bp_net_tile_width()
+  t = ((n + 3) // 4 + 63) // 64 * 64
+  return max(1024, min(cap, t))
+
+
 class EINetwork:
   """One E/I COBA network: n neurons, [0, n_exc) excitatory, shared LIF parameters.
 
@@ -66,8 +75,10 @@ class EINetwork:
   four EventJitFPHomoLinear projections of BrainPy, outdim_parallel=True)."""
 
   def __init__(self, n, n_exc, *, indices=None, indptr=None, we=0.6, wi=6.7, params: Optional[LifParams] = None,
-               jitconn=None, device=None, V0=None):
+               jitconn=None, device=None, V0=None, net_tile=None):
     self.n, self.n_exc = int(n), int(n_exc)
+    # neurons per CTA in the cluster runner (multiple of 64, at most bp_net_tile_width())
+    self.net_tile = int(net_tile) if net_tile is not None else None
     self.we, self.wi = float(we), float(wi)
     self.params = params or LifParams()
     self.device = device or torch.device("cuda", torch.cuda.current_device())
@@ -90,7 +101,8 @@ class EINetwork:
 
   # ---- construction helpers ---------------------------------------------------------
   @classmethod
-  def fixed_prob(cls, n_exc, n_inh, prob=0.02, we=0.6, wi=6.7, seed=0, params=None, device=None, V0=None):
+  def fixed_prob(cls, n_exc, n_inh, prob=0.02, we=0.6, wi=6.7, seed=0, params=None, device=None, V0=None,
+                 net_tile=None):
     """COBA.py's four FixedProb(prob) projections with fan-out int(post*prob) per group,
     merged into one n x n CSR (E rows: E targets then I targets; I rows likewise)."""
     dev = device or torch.device("cuda", torch.cuda.current_device())
@@ -105,7 +117,8 @@ class EINetwork:
     k_row = int(n_exc * prob) + int(n_inh * prob)
     indices = torch.cat(blocks).to(torch.int32)
     indptr = (torch.arange(n + 1, device=dev, dtype=torch.int64) * k_row).to(torch.int32)
-    return cls(n, n_exc, indices=indices, indptr=indptr, we=we, wi=wi, params=params, device=dev, V0=V0)
+    return cls(n, n_exc, indices=indices, indptr=indptr, we=we, wi=wi, params=params, device=dev, V0=V0,
+               net_tile=net_tile)
 
   def reset_state(self, V, ge, gi, t_last, spike, t_step=0):
     """Overwrites the state (tensors of length n) and the time index."""
@@ -123,7 +136,9 @@ class EINetwork:
   # ---- persistent cluster form --------------------------------------------------------
   def _cluster_plan(self):
     if self._plan is None:
-      tw = _lib.lib().bp_net_tile_width()
+      tw = self.net_tile or default_net_tile(self.n)
+      if tw % 64 or not 64 <= tw <= _lib.lib().bp_net_tile_width():
+        raise ValueError(f"net_tile {tw} must be a multiple of 64 in [64, {_lib.lib().bp_net_tile_width()}]")
       self._plan = _event.CSRPlan(self.indices, self.indptr, (self.n, self.n), tile_w=tw, cluster=1)
       if self._plan.c.n_tiles > _lib.lib().bp_net_max_tiles():
         raise ValueError(f"network of {self.n} neurons exceeds one cluster ({_lib.lib().bp_net_max_tiles()} tiles)")

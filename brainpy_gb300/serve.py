@@ -202,6 +202,13 @@ def bench(args):
   """Serving loop on a bounded sample of the job stream (sizes 4k-1M log-uniform, durations
   100-2000 ms, Poisson 50 jobs/s, HBM budget 150 GB)."""
   n_jobs = args.nets if args.nets != 256 else 60
+  # warm-up session (a server in service is warm): a few short jobs of every kind and size class
+  warm = Server(hbm_budget_bytes=150e9)
+  for k, (n, conn) in enumerate([(5000, "csr"), (200_000, "csr"), (5000, "jitconn"), (200_000, "jitconn")]):
+    warm.submit(Job(jid=k, n=n, conn=conn, duration_ms=20.0, we=0.6, wi=6.7, arrival=0.0, seed=7 + k))
+  warm.run()
+  del warm
+  torch.cuda.synchronize()
   jobs = poisson_jobs(n_jobs)
   srv = Server(hbm_budget_bytes=150e9)
   for j in jobs:
@@ -209,6 +216,26 @@ def bench(args):
   wall = srv.run()
   lat = np.array([j.latency for j in srv.done])
   steps = sum(j.steps_total for j in srv.done)
+  # the plain per-network path on the same jobs: one job at a time, one kernel per operator per
+  # step from a host loop, a bounded number of steps per job (after one warm-up step)
+  # (each job's per-step time, weighted by the job's length as in the served run)
+  k_plain = 20
+  sample = poisson_jobs(n_jobs)[: min(n_jobs, 12)]
+  plain_steps, plain_t = 0, 0.0
+  for job in sample:
+    net = build_job(job, srv.device)
+    net.run(1, method="ops")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    net.run(k_plain, method="ops")
+    torch.cuda.synchronize()
+    per_step = (time.perf_counter() - t0) / k_plain
+    n_steps = int(round(job.duration_ms / srv.dt))
+    plain_t += per_step * n_steps
+    plain_steps += n_steps
+    del net
+  torch.cuda.empty_cache()
+  plain = plain_steps / plain_t
   return {"metric": "served job latency p50 (COBA jobs, continuous batching)", "value": float(np.percentile(lat, 50)),
           "unit": "s", "n_gpus": 1, "steps": steps, "warmup": 0, "ms_per_step": None, "higher_is_better": False,
           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -216,4 +243,9 @@ def bench(args):
                                  "jitconn fan-out 1000, durations U[100,2000] ms, HBM budget 150 GB"},
           "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
           "jobs_done": len(srv.done), "wall_s": wall, "synaptic_events_per_s": srv.events / wall,
-          "network_steps_per_s": steps / wall}
+          "network_steps_per_s": steps / wall,
+          "plain_per_network_path": {"value": plain, "unit": "network-steps/s",
+                                     "sample": f"the first {len(sample)} jobs of the stream, one at a time, per-operator "
+                                               f"kernels from a host loop; {k_plain} steps timed per job, "
+                                               "weighted by the job's length"},
+          "speedup_vs_plain": (steps / wall) / plain}

@@ -43,11 +43,12 @@ def parse():
   ap.add_argument("--no-cpu-baseline", action="store_true")
   ap.add_argument("--cpu-seconds", type=float, default=12.0)
   ap.add_argument("--workload", default="event_csrmv",
-                  choices=["event_csrmv", "coba", "batched", "jitconn_net", "serve", "sweep"],
+                  choices=["event_csrmv", "coba", "batched", "jitconn_net", "serve", "sweep", "vmap"],
                   help="event_csrmv (headline); coba: the 4000-neuron COBA example; batched: 256 uneven "
                        "networks in persistent cluster launches vs the plain per-network path; jitconn_net: "
                        "4M-neuron just-in-time network; serve: continuous-batching serving loop; sweep: the "
-                       "operator sweep (event/sparse csrmv, jitconn) as one JSON line")
+                       "operator sweep (event/sparse csrmv, jitconn) as one JSON line; vmap: a batch of 8 "
+                       "spike vectors through one matrix in one launch pair vs 8 sequential calls")
   ap.add_argument("--nets", type=int, default=256)
   ap.add_argument("--sim-steps", type=int, default=0, help="override the workload's number of steps")
   return ap.parse_args()
@@ -195,7 +196,7 @@ def main():
   args = parse()
   if args.workload != "event_csrmv":
     fn = {"coba": bench_coba, "batched": bench_batched, "jitconn_net": bench_jitconn_net, "serve": bench_serve,
-          "sweep": bench_sweep}
+          "sweep": bench_sweep, "vmap": bench_vmap}
     line = fn[args.workload](args)
     if line is not None:
       print(json.dumps(line))
@@ -607,6 +608,44 @@ def bench_sweep(args):
           "config": {"workload": "operator sweep; value = event.csrmv T N=1e6 K=1000 r=2% homo",
                      "l2": "flushed before each replay", "timing": "CUDA-graph replay, CUDA events"},
           "points": pts}
+
+
+def bench_vmap(args, batch=8):
+  """A batch of spike vectors through one matrix (the reference maps its primitive over a batch
+  with a sequential scan of single calls, brainpy/_src/math/op_register/utils.py:16-38):
+  one launch pair for the batch (CSRPlan.csrmv_batch) against `batch` sequential single calls,
+  both as CUDA graphs, L2 flushed before each replay."""
+  from brainpy_gb300.connect import bernoulli_events, fixed_prob_csr
+  from brainpy_gb300.math import event
+  n, k = args.n, args.fanout
+  ind, ptr = fixed_prob_csr(n, n, k, seed=0)
+  plan = event.prepare(ind, ptr, shape=(n, n))
+  w = torch.ones(1, device="cuda")
+  ev = torch.stack([bernoulli_events(n, args.rate, seed=2 + b) for b in range(batch)])
+  active = int(ev.sum())
+  out_b = torch.empty((batch, n), device="cuda")
+  out_s = torch.empty((batch, n), device="cuda")
+
+  def batched():
+    plan.csrmv_batch(ev, w, out=out_b)
+
+  def sequential():
+    for b in range(batch):
+      plan.csrmv(ev[b], w, out=out_s[b])
+
+  flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+  t_b = _graph_time(batched, flush_buf, steps=max(args.steps, 20))
+  t_s = _graph_time(sequential, flush_buf, steps=max(args.steps, 20))
+  torch.cuda.synchronize()
+  assert torch.equal(out_b, out_s), "batched rows differ from single calls"
+  e = active * k
+  return {"metric": "event.csrmv transpose, batch of spike vectors (events/s)", "value": e / t_b, "unit": "events/s",
+          "n_gpus": 1, "steps": max(args.steps, 20), "warmup": 3, "ms_per_step": t_b * 1e3, "higher_is_better": True,
+          "scaling": "weak", "vs_baseline": None, "dtype": "u32 counts", "data": "synthetic",
+          "config": {"workload": f"N={n} K={k} rate={args.rate} homo, batch of {batch} Bernoulli spike vectors",
+                     "l2": "flushed before each replay", "timing": "CUDA-graph replay, CUDA events"},
+          "sequential_calls": {"value": e / t_s, "ms_per_step": t_s * 1e3},
+          "speedup_vs_sequential": t_s / t_b, "gpu_launches": 2}
 
 
 def launches_per_step(args):

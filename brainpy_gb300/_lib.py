@@ -39,6 +39,8 @@ SIGNATURES = {
     "bp_csrmv": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_ptr, _c_i64, _c_i64, _c_i32, _c_ptr,
                           _c_ptr]),
     "bp_csr_to_coo": (_c_i32, [_c_ptr, _c_i32, _c_i64, _c_i64, _c_ptr, _c_ptr]),
+    "bp_csr_sampled_outer": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_ptr,
+                                      _c_ptr]),
     "bp_csr_to_dense": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_ptr, _c_ptr]),
     "bp_jitconn_mv": (_c_i32, [_c_i32, _c_i32, _c_ptr, _c_i64, _c_i64, _c_f32, _c_f32, _c_i32, _c_u32, _c_i32, _c_i32,
                                _c_ptr, _c_ptr]),
@@ -51,6 +53,10 @@ SIGNATURES = {
     "bp_event_csrmv_planned_workspace_size": (_c_size, [_c_ptr]),
     "bp_event_csrmv_planned": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_i32, _c_ptr, _c_i32, _c_ptr, _c_size, _c_ptr]),
     "bp_csrmv_planned": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i32, _c_ptr, _c_size, _c_ptr]),
+    "bp_event_csrmv_planned_batch_workspace_size": (_c_size, [_c_ptr, _c_i32]),
+    "bp_event_csrmv_planned_batch": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_i32, _c_i32, _c_ptr, _c_i32, _c_ptr, _c_size,
+                                              _c_ptr]),
+    "bp_csrmv_planned_batch": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_i32, _c_ptr, _c_i32, _c_ptr, _c_size, _c_ptr]),
     "bp_csr_plan_arrays": (_c_i32, [_c_ptr, ctypes.POINTER(_c_ptr), ctypes.POINTER(_c_ptr), ctypes.POINTER(_c_ptr)]),
     "bp_lif_coba_step": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i32,
                                   _c_f32, _c_ptr]),

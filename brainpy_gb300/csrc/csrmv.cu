@@ -111,6 +111,37 @@ __global__ void __launch_bounds__(256) csr_dense_kernel(const float* __restrict_
   }
 }
 
+// The weight cotangent of the CSR products (brainpy/_src/math/event/_csr_matvec.py:545-547,
+// brainpy/_src/math/sparse/_csr_mv.py:237-239): out[j] = x[i] * y[indices[j]] for every stored
+// entry j of row i, 0 where the column is out of range.  One warp per row, coalesced index
+// stream and output, gathers of y.  Entries outside every row ([0, indptr[0]) and
+// [indptr[m], nnz)) are set to 0.
+template <typename IdxT>
+__global__ void __launch_bounds__(256) csr_sampled_outer_kernel(const IdxT* __restrict__ indptr,
+                                                                const IdxT* __restrict__ indices, int64_t nnz,
+                                                                int64_t m, int64_t n, const float* __restrict__ x,
+                                                                const float* __restrict__ y, float* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (gw == 0) {
+    int64_t b0 = (int64_t)indptr[0], em = (int64_t)indptr[m];
+    b0 = b0 < 0 ? 0 : (b0 > nnz ? nnz : b0);
+    em = em < b0 ? b0 : (em > nnz ? nnz : em);
+    for (int64_t j = lane; j < b0; j += 32) out[j] = 0.0f;
+    for (int64_t j = em + lane; j < nnz; j += 32) out[j] = 0.0f;
+  }
+  for (int64_t row = gw; row < m; row += nwarps) {
+    int64_t b, e;
+    csr_row_bounds(indptr, row, nnz, b, e);
+    const float xv = __ldg(x + row);
+    for (int64_t j = b + lane; j < e; j += 32) {
+      const int64_t c = (int64_t)indices[j];
+      out[j] = (uint64_t)c < (uint64_t)n ? __fmul_rn(xv, __ldg(y + c)) : 0.0f;
+    }
+  }
+}
+
 static int grid_rows(int64_t m) {
   int64_t g = (m + 7) / 8;
   const int64_t maxb = (int64_t)device_sm_count() * 32;
@@ -170,6 +201,30 @@ bp_status bp_csrmv(const float* data, int64_t ndata, const void* indices, const 
 }  // extern "C"
 
 extern "C" {
+
+bp_status bp_csr_sampled_outer(const float* x, const float* y, const void* indices, const void* indptr,
+                               bp_itype itype, int64_t nnz, int64_t m, int64_t n, float* out, bp_stream_t stream) {
+  clear_error();
+  cudaStream_t st = as_cuda(stream);
+  BP_REQUIRE(m >= 0 && n >= 0 && nnz >= 0, BP_EINVAL, "csr_sampled_outer: negative size");
+  BP_REQUIRE(itype == BP_I32 || itype == BP_I64, BP_EDTYPE, "csr_sampled_outer: bad index type %d", (int)itype);
+  if (nnz == 0) return BP_OK;
+  BP_REQUIRE(out != nullptr, BP_EINVAL, "csr_sampled_outer: null out");
+  if (m == 0) {
+    BP_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * (size_t)nnz, st));
+    return BP_OK;
+  }
+  BP_REQUIRE(x && indices && indptr && (y || n == 0), BP_EINVAL, "csr_sampled_outer: null pointer");
+  const int g = grid_rows(m);
+  ScopedKernelTimer tk(st);
+  if (itype == BP_I32)
+    csr_sampled_outer_kernel<int32_t><<<g, 256, 0, st>>>(static_cast<const int32_t*>(indptr),
+                                                         static_cast<const int32_t*>(indices), nnz, m, n, x, y, out);
+  else
+    csr_sampled_outer_kernel<int64_t><<<g, 256, 0, st>>>(static_cast<const int64_t*>(indptr),
+                                                         static_cast<const int64_t*>(indices), nnz, m, n, x, y, out);
+  return check_launch("csr_sampled_outer_kernel");
+}
 
 bp_status bp_csr_to_coo(const void* indptr, bp_itype itype, int64_t m, int64_t nnz, void* rows, bp_stream_t stream) {
   clear_error();

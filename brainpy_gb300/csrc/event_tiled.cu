@@ -98,13 +98,21 @@ __global__ void __launch_bounds__(256) plan_build_kernel(const IdxT* __restrict_
 // ---------------------------------------------------------------------------
 // blocked compaction: block b handles rows [b*4096, (b+1)*4096)
 // ---------------------------------------------------------------------------
-template <int ET>
+template <int ET, bool BATCH>
 __global__ void __launch_bounds__(256) compact_blocked_kernel(const void* __restrict__ events, int64_t m,
                                                               int32_t* __restrict__ lists,
                                                               int32_t* __restrict__ counts) {
   // let the accumulation kernel launch and zero its shared memory while this grid runs;
   // it reads lists/counts only after cudaGridDependencySynchronize()
   cudaTriggerProgrammaticLaunchCompletion();
+  // vector blockIdx.y of a batch: rows of m events, lists of gridDim.x * 4096, counts of gridDim.x
+  // (a separate instantiation: the offsets cost measurable time in the single-vector call)
+  if (BATCH) {
+    const int64_t b = blockIdx.y;
+    events = static_cast<const char*>(events) + b * m * (ET == BP_EV_BOOL ? 1 : 4);
+    lists += b * (int64_t)gridDim.x * kCompactRows;
+    counts += b * (int64_t)gridDim.x;
+  }
   const bool vec_ok = ((reinterpret_cast<uintptr_t>(events) & 15u) == 0);
   const int64_t blk0 = (int64_t)blockIdx.x * kCompactRows;
   const int64_t base = blk0 + (int64_t)threadIdx.x * 16;
@@ -189,9 +197,10 @@ struct TiledArgs {
   const float* w_homo;
   const float* row_val;  // dense vector for kRowVal / kWRow
   float* out;
-  int64_t n;
+  int64_t m, n;  // a batch of vectors: row_val rows of m, out rows of n
   int32_t tile_w, n_tiles, nb, acc_words;
-  int32_t vec_out;  // out is 16-byte aligned (tile_w is a multiple of 4)
+  int32_t batch;    // vectors per launch: gridDim.y
+  int32_t vec_out;  // every vector's out row is 16-byte aligned (tile_w is a multiple of 4)
 };
 
 // Warp-independent processing: after one CTA-wide prefix over this rank's compaction blocks,
@@ -202,7 +211,7 @@ struct TiledArgs {
 // lanes take one segment each (lane gl loads 16-byte chunks gl, gl + G, ... -- RND rounds, 8
 // tile-local indices per chunk) and UB segments per group are loaded back to back before any
 // shared-memory atomic is issued.
-template <int MODE, int G, int RND, bool PF>
+template <int MODE, int G, int RND, bool PF, bool BATCH>
 __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const TiledArgs a) {
   constexpr bool HAS_W = (MODE == kWeight || MODE == kWRow);
   constexpr bool HAS_X = (MODE == kRowVal || MODE == kWRow);
@@ -218,6 +227,11 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const Ti
   const int R = (int)cluster.num_blocks();
   const int rank = (int)cluster.block_rank();
   const int tile = blockIdx.x / R;
+  // vector blockIdx.y of a batch (a separate instantiation: the offsets cost measurable time
+  // in the single-vector call)
+  const int32_t* __restrict__ lists = BATCH ? a.lists + (int64_t)blockIdx.y * a.nb * kCompactRows : a.lists;
+  const int32_t* __restrict__ counts = BATCH ? a.counts + (int64_t)blockIdx.y * a.nb : a.counts;
+  const float* __restrict__ row_val = (BATCH && HAS_X) ? a.row_val + (int64_t)blockIdx.y * a.m : a.row_val;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
 
@@ -235,7 +249,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const Ti
   for (int g0 = b0; g0 < b1; g0 += kBlockGroup) {
     const int ng = min(kBlockGroup, b1 - g0);
     __syncthreads();  // s_boff of the previous group is no longer read
-    int v = tid < ng ? a.counts[g0 + tid] : 0;
+    int v = tid < ng ? counts[g0 + tid] : 0;
     int incl = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -275,7 +289,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const Ti
       const int g = (k << 5) + lane;
       if (k >= nslices || g >= total) return -1;
       while (s_boff[blk + 1] <= g) ++blk;  // blocks hold ~rate*4096 rows: a step or two
-      return __ldg(a.lists + (int64_t)(g0 + blk) * kCompactRows + (g - s_boff[blk]));
+      return __ldg(lists + (int64_t)(g0 + blk) * kCompactRows + (g - s_boff[blk]));
     };
     auto fetch_desc = [&](int32_t row, uint32_t& st, uint32_t& nch, float& xv) {
       st = 0;
@@ -285,7 +299,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const Ti
         const uint32_t* so = a.seg_off + (int64_t)row * so_stride + tile;
         st = __ldg(so);
         nch = __ldg(so + 1) - st;
-        if (HAS_X) xv = __ldg(a.row_val + row);
+        if (HAS_X) xv = __ldg(row_val + row);
       }
     };
 
@@ -396,6 +410,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const Ti
   const int c0 = rank * slice;
   const float w = (MODE == kCount || MODE == kRowVal) ? __ldg(a.w_homo) : 0.0f;
   const int64_t col_base = (int64_t)tile * a.tile_w;
+  float* __restrict__ out = BATCH ? a.out + (int64_t)blockIdx.y * a.n : a.out;
   for (int c = c0 + 4 * tid; c < c0 + slice; c += 4 * nthr) {
     uint4 x[8];
 #pragma unroll
@@ -441,10 +456,10 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const Ti
     }
     const int64_t gc = col_base + c;
     if (a.vec_out && c + 3 < a.tile_w && gc + 3 < a.n) {
-      *reinterpret_cast<float4*>(a.out + gc) = make_float4(o[0], o[1], o[2], o[3]);
+      *reinterpret_cast<float4*>(out + gc) = make_float4(o[0], o[1], o[2], o[3]);
     } else {
       for (int q = 0; q < 4; ++q)
-        if (c + q < a.tile_w && gc + q < a.n) a.out[gc + q] = o[q];
+        if (c + q < a.tile_w && gc + q < a.n) out[gc + q] = o[q];
     }
   }
   cluster.sync();
@@ -487,13 +502,13 @@ static cudaError_t prepare_kernel(K kfn, bool* done) {
   return e;
 }
 
-template <int MODE, int G, int RND, bool PF>
+template <int MODE, int G, int RND, bool PF, bool BATCH = false>
 static bp_status launch_tiled_g(const TiledArgs& a, int R, cudaStream_t st) {
-  auto kfn = ecsr_t_tiled_kernel<MODE, G, RND, PF>;
+  auto kfn = ecsr_t_tiled_kernel<MODE, G, RND, PF, BATCH>;
   static bool done[64] = {false};
   BP_CUDA_TRY(prepare_kernel(kfn, done));
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)(a.n_tiles * R), 1, 1);
+  cfg.gridDim = dim3((unsigned)(a.n_tiles * R), (unsigned)a.batch, 1);
   cfg.blockDim = dim3(kTiledThreads, 1, 1);
   cfg.dynamicSmemBytes = tiled_smem_bytes(a.acc_words);
   cfg.stream = st;
@@ -536,9 +551,11 @@ template <int MODE>
 static bp_status launch_tiled(const TiledArgs& a, int R, double chunks, cudaStream_t st) {
   int G, RND, PF;
   tiled_config(chunks, G, RND, PF);
-#define BP_TILED_CASE(g, r)                                                                   \
-  if (G == g && RND == r)                                                                     \
-    return PF ? launch_tiled_g<MODE, g, r, true>(a, R, st) : launch_tiled_g<MODE, g, r, false>(a, R, st);
+#define BP_TILED_CASE(g, r)                                                                           \
+  if (G == g && RND == r) {                                                                           \
+    if (a.batch > 1) return launch_tiled_g<MODE, g, r, false, true>(a, R, st);                        \
+    return PF ? launch_tiled_g<MODE, g, r, true>(a, R, st) : launch_tiled_g<MODE, g, r, false>(a, R, st); \
+  }
   BP_TILED_CASE(1, 1)
   BP_TILED_CASE(2, 1)
   BP_TILED_CASE(4, 1)
@@ -551,26 +568,27 @@ static bp_status launch_tiled(const TiledArgs& a, int R, double chunks, cudaStre
 }
 
 template <int ET>
-static bp_status launch_compact_blocked(const void* events, int64_t m, int32_t* lists, int32_t* counts,
+static bp_status launch_compact_blocked(const void* events, int64_t m, int batch, int32_t* lists, int32_t* counts,
                                         cudaStream_t st) {
   int nb = (int)((m + kCompactRows - 1) / kCompactRows);
-  compact_blocked_kernel<ET><<<nb, 256, 0, st>>>(events, m, lists, counts);
+  if (batch > 1) compact_blocked_kernel<ET, true><<<dim3(nb, batch), 256, 0, st>>>(events, m, lists, counts);
+  else compact_blocked_kernel<ET, false><<<nb, 256, 0, st>>>(events, m, lists, counts);
   return check_launch("compact_blocked_kernel");
 }
 
-static bp_status compact_blocked(const void* events, bp_etype et, int64_t m, int32_t* lists, int32_t* counts,
-                                 cudaStream_t st) {
+static bp_status compact_blocked(const void* events, bp_etype et, int64_t m, int batch, int32_t* lists,
+                                 int32_t* counts, cudaStream_t st) {
   switch (et) {
-    case BP_EV_BOOL: return launch_compact_blocked<BP_EV_BOOL>(events, m, lists, counts, st);
-    case BP_EV_F32_POS: return launch_compact_blocked<BP_EV_F32_POS>(events, m, lists, counts, st);
-    case BP_EV_F32_NZ: return launch_compact_blocked<BP_EV_F32_NZ>(events, m, lists, counts, st);
+    case BP_EV_BOOL: return launch_compact_blocked<BP_EV_BOOL>(events, m, batch, lists, counts, st);
+    case BP_EV_F32_POS: return launch_compact_blocked<BP_EV_F32_POS>(events, m, batch, lists, counts, st);
+    case BP_EV_F32_NZ: return launch_compact_blocked<BP_EV_F32_NZ>(events, m, batch, lists, counts, st);
   }
   return BP_EINVAL;
 }
 
 // how many clusters of R CTAs with `smem` bytes of shared memory can be resident at once
 static int max_active_clusters(int R, size_t smem) {
-  auto kfn = ecsr_t_tiled_kernel<kCount, 4, 1, true>;
+  auto kfn = ecsr_t_tiled_kernel<kCount, 4, 1, true, false>;
   static bool done[64] = {false};
   if (prepare_kernel(kfn, done) != cudaSuccess) {
     cudaGetLastError();
@@ -606,6 +624,8 @@ static bp_status tiled_args_from_plan(const bp_csr_plan* plan, int cluster, Tile
   a.seg_off = v.seg_off;
   a.idx = v.idx;
   a.w = v.w;
+  a.batch = 1;
+  a.m = plan->m;
   a.n = plan->n;
   a.tile_w = plan->tile_w;
   a.n_tiles = plan->n_tiles;
@@ -714,53 +734,84 @@ bp_status bp_csr_plan_arrays(const bp_csr_plan* plan, const uint32_t** seg_off, 
   return BP_OK;
 }
 
-size_t bp_event_csrmv_planned_workspace_size(const bp_csr_plan* plan) {
-  if (!plan || plan->m <= 0) return 256;
-  int64_t nb = (plan->m + kCompactRows - 1) / kCompactRows;
-  return align_up(sizeof(int32_t) * (size_t)nb * kCompactRows, 256) + align_up(sizeof(int32_t) * (size_t)nb, 256);
+size_t bp_event_csrmv_planned_batch_workspace_size(const bp_csr_plan* plan, int32_t batch) {
+  if (!plan || plan->m <= 0 || batch <= 0) return 256;
+  const int64_t nb = (plan->m + kCompactRows - 1) / kCompactRows;
+  return align_up(sizeof(int32_t) * (size_t)batch * (size_t)nb * kCompactRows, 256) +
+         align_up(sizeof(int32_t) * (size_t)batch * (size_t)nb, 256);
 }
+
+size_t bp_event_csrmv_planned_workspace_size(const bp_csr_plan* plan) {
+  return bp_event_csrmv_planned_batch_workspace_size(plan, 1);
+}
+
+}  // extern "C"
+
+namespace bp {
+
+// One launch pair for `batch` vectors: vectors (events or dense values) are rows of m, outputs
+// rows of n, both contiguous.  `dense` selects sparse.csrmv semantics (vec != 0 rows carry their
+// value) over event semantics.
+static bp_status planned_batch(const char* who, const bp_csr_plan* plan, const float* w_homo, const void* vec,
+                               bp_etype etype, bool dense, int32_t batch, float* out, int32_t cluster,
+                               void* workspace, size_t workspace_bytes, cudaStream_t st) {
+  BP_REQUIRE(plan != nullptr && plan->mem != nullptr, BP_EINVAL, "%s: null plan", who);
+  BP_REQUIRE(etype >= BP_EV_BOOL && etype <= BP_EV_F32_NZ, BP_EDTYPE, "%s: bad event type %d", who, (int)etype);
+  BP_REQUIRE(batch >= 0 && batch <= 65535, BP_EINVAL, "%s: batch must be in [0, 65535] (got %d)", who, batch);
+  if (cluster == 0) cluster = 4;
+  BP_REQUIRE(cluster == 1 || cluster == 2 || cluster == 4 || cluster == 8, BP_EINVAL,
+             "%s: cluster must be 1, 2, 4 or 8 (got %d)", who, cluster);
+  const int64_t m = plan->m, n = plan->n;
+  if (n == 0 || batch == 0) return BP_OK;
+  BP_REQUIRE(out != nullptr, BP_EINVAL, "%s: null out", who);
+  if (m == 0 || plan->nnz == 0) {
+    BP_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * (size_t)n * (size_t)batch, st));
+    return BP_OK;
+  }
+  BP_REQUIRE(vec != nullptr, BP_EINVAL, "%s: null %s", who, dense ? "vector" : "events");
+  const bool homo = plan->heter == 0;
+  BP_REQUIRE(!homo || w_homo != nullptr, BP_EINVAL, "%s: homogeneous plan needs w_homo", who);
+  const size_t need = bp_event_csrmv_planned_batch_workspace_size(plan, batch);
+  BP_REQUIRE(workspace && workspace_bytes >= need, BP_ENOMEM, "%s: workspace %zu < %zu", who, workspace_bytes, need);
+  TiledArgs a;
+  double chunks = 0.0;
+  bp_status s = tiled_args_from_plan(plan, cluster, a, chunks, who);
+  if (s != BP_OK) return s;
+  int32_t* lists = static_cast<int32_t*>(workspace);
+  int32_t* counts = reinterpret_cast<int32_t*>(
+      static_cast<char*>(workspace) + align_up(sizeof(int32_t) * (size_t)batch * (size_t)a.nb * kCompactRows, 256));
+  ScopedKernelTimer tk(st);  // brackets both kernels of the call
+  s = compact_blocked(vec, dense ? BP_EV_F32_NZ : etype, m, batch, lists, counts, st);
+  if (s != BP_OK) return s;
+  a.lists = lists;
+  a.counts = counts;
+  a.w_homo = w_homo;
+  a.row_val = dense ? static_cast<const float*>(vec) : nullptr;
+  a.out = out;
+  a.batch = batch;
+  a.vec_out = ((reinterpret_cast<uintptr_t>(out) & 15u) == 0 && (batch == 1 || (n & 3) == 0)) ? 1 : 0;
+  if (dense) return homo ? launch_tiled<kRowVal>(a, cluster, chunks, st) : launch_tiled<kWRow>(a, cluster, chunks, st);
+  return homo ? launch_tiled<kCount>(a, cluster, chunks, st) : launch_tiled<kWeight>(a, cluster, chunks, st);
+}
+
+}  // namespace bp
+
+extern "C" {
 
 bp_status bp_event_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, const void* events, bp_etype etype,
                                  float* out, int32_t cluster, void* workspace, size_t workspace_bytes,
                                  bp_stream_t stream) {
   clear_error();
-  cudaStream_t st = as_cuda(stream);
-  BP_REQUIRE(plan != nullptr && plan->mem != nullptr, BP_EINVAL, "event_csrmv_planned: null plan");
-  BP_REQUIRE(etype >= BP_EV_BOOL && etype <= BP_EV_F32_NZ, BP_EDTYPE, "event_csrmv_planned: bad event type %d",
-             (int)etype);
-  if (cluster == 0) cluster = 4;
-  BP_REQUIRE(cluster == 1 || cluster == 2 || cluster == 4 || cluster == 8, BP_EINVAL,
-             "event_csrmv_planned: cluster must be 1, 2, 4 or 8 (got %d)", cluster);
-  const int64_t m = plan->m, n = plan->n;
-  if (n == 0) return BP_OK;
-  BP_REQUIRE(out != nullptr, BP_EINVAL, "event_csrmv_planned: null out");
-  if (m == 0 || plan->nnz == 0) {
-    BP_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * (size_t)n, st));
-    return BP_OK;
-  }
-  BP_REQUIRE(events != nullptr, BP_EINVAL, "event_csrmv_planned: null events");
-  const bool homo = plan->heter == 0;
-  BP_REQUIRE(!homo || w_homo != nullptr, BP_EINVAL, "event_csrmv_planned: homogeneous plan needs w_homo");
-  BP_REQUIRE(workspace && workspace_bytes >= bp_event_csrmv_planned_workspace_size(plan), BP_ENOMEM,
-             "event_csrmv_planned: workspace %zu < %zu", workspace_bytes,
-             bp_event_csrmv_planned_workspace_size(plan));
-  TiledArgs a;
-  double chunks = 0.0;
-  bp_status s = tiled_args_from_plan(plan, cluster, a, chunks, "event_csrmv_planned");
-  if (s != BP_OK) return s;
-  int32_t* lists = static_cast<int32_t*>(workspace);
-  int32_t* counts = reinterpret_cast<int32_t*>(static_cast<char*>(workspace) +
-                                               align_up(sizeof(int32_t) * (size_t)a.nb * kCompactRows, 256));
-  ScopedKernelTimer tk(st);  // brackets both kernels of the call
-  s = compact_blocked(events, etype, m, lists, counts, st);
-  if (s != BP_OK) return s;
-  a.lists = lists;
-  a.counts = counts;
-  a.w_homo = w_homo;
-  a.row_val = nullptr;
-  a.out = out;
-  a.vec_out = ((reinterpret_cast<uintptr_t>(out) & 15u) == 0) ? 1 : 0;
-  return homo ? launch_tiled<kCount>(a, cluster, chunks, st) : launch_tiled<kWeight>(a, cluster, chunks, st);
+  return planned_batch("event_csrmv_planned", plan, w_homo, events, etype, false, 1, out, cluster, workspace,
+                       workspace_bytes, as_cuda(stream));
+}
+
+bp_status bp_event_csrmv_planned_batch(const bp_csr_plan* plan, const float* w_homo, const void* events,
+                                       bp_etype etype, int32_t batch, float* out, int32_t cluster, void* workspace,
+                                       size_t workspace_bytes, bp_stream_t stream) {
+  clear_error();
+  return planned_batch("event_csrmv_planned_batch", plan, w_homo, events, etype, false, batch, out, cluster,
+                       workspace, workspace_bytes, as_cuda(stream));
 }
 
 // sparse.csrmv, transpose=1, on a plan: out[j] = sum_i A[i, j] * vec[i].  Rows with vec[i] == 0
@@ -769,40 +820,16 @@ bp_status bp_event_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, c
 bp_status bp_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, const float* vec, float* out,
                            int32_t cluster, void* workspace, size_t workspace_bytes, bp_stream_t stream) {
   clear_error();
-  cudaStream_t st = as_cuda(stream);
-  BP_REQUIRE(plan != nullptr && plan->mem != nullptr, BP_EINVAL, "csrmv_planned: null plan");
-  if (cluster == 0) cluster = 4;
-  BP_REQUIRE(cluster == 1 || cluster == 2 || cluster == 4 || cluster == 8, BP_EINVAL,
-             "csrmv_planned: cluster must be 1, 2, 4 or 8 (got %d)", cluster);
-  const int64_t m = plan->m, n = plan->n;
-  if (n == 0) return BP_OK;
-  BP_REQUIRE(out != nullptr, BP_EINVAL, "csrmv_planned: null out");
-  if (m == 0 || plan->nnz == 0) {
-    BP_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * (size_t)n, st));
-    return BP_OK;
-  }
-  BP_REQUIRE(vec != nullptr, BP_EINVAL, "csrmv_planned: null vector");
-  const bool homo = plan->heter == 0;
-  BP_REQUIRE(!homo || w_homo != nullptr, BP_EINVAL, "csrmv_planned: homogeneous plan needs w_homo");
-  BP_REQUIRE(workspace && workspace_bytes >= bp_event_csrmv_planned_workspace_size(plan), BP_ENOMEM,
-             "csrmv_planned: workspace %zu < %zu", workspace_bytes, bp_event_csrmv_planned_workspace_size(plan));
-  TiledArgs a;
-  double chunks = 0.0;
-  bp_status s = tiled_args_from_plan(plan, cluster, a, chunks, "csrmv_planned");
-  if (s != BP_OK) return s;
-  int32_t* lists = static_cast<int32_t*>(workspace);
-  int32_t* counts = reinterpret_cast<int32_t*>(static_cast<char*>(workspace) +
-                                               align_up(sizeof(int32_t) * (size_t)a.nb * kCompactRows, 256));
-  ScopedKernelTimer tk(st);
-  s = compact_blocked(vec, BP_EV_F32_NZ, m, lists, counts, st);
-  if (s != BP_OK) return s;
-  a.lists = lists;
-  a.counts = counts;
-  a.w_homo = w_homo;
-  a.row_val = vec;
-  a.out = out;
-  a.vec_out = ((reinterpret_cast<uintptr_t>(out) & 15u) == 0) ? 1 : 0;
-  return homo ? launch_tiled<kRowVal>(a, cluster, chunks, st) : launch_tiled<kWRow>(a, cluster, chunks, st);
+  return planned_batch("csrmv_planned", plan, w_homo, vec, BP_EV_F32_NZ, true, 1, out, cluster, workspace,
+                       workspace_bytes, as_cuda(stream));
+}
+
+bp_status bp_csrmv_planned_batch(const bp_csr_plan* plan, const float* w_homo, const float* vec, int32_t batch,
+                                 float* out, int32_t cluster, void* workspace, size_t workspace_bytes,
+                                 bp_stream_t stream) {
+  clear_error();
+  return planned_batch("csrmv_planned_batch", plan, w_homo, vec, BP_EV_F32_NZ, true, batch, out, cluster,
+                       workspace, workspace_bytes, as_cuda(stream));
 }
 
 }  // extern "C"

@@ -6,8 +6,9 @@ Same constructor arguments and `update` semantics: CSR layers take the connectio
 (indices, indptr) -- from `conn.require('csr')` when given a BrainPy-style connector -- with
 shape (pre_num, post_num) and transpose=True by default; just-in-time layers use
 shape=(num_out, num_in) and outdim_parallel = not atomic.  Inputs of more than one dimension
-are treated as a batch of vectors along the last axis.  Training modes, sharding and
-synaptic plasticity are not part of this package.
+are treated as a batch of vectors along the last axis (one launch pair for a planned CSR
+product).  Weights given as tensors that require a gradient are trained through the operators'
+differentiation rules; sharding and synaptic plasticity are not part of this package.
 """
 from typing import Optional
 
@@ -23,16 +24,20 @@ __all__ = ["CSRLinear", "EventCSRLinear", "JitFPHomoLinear", "JitFPUniformLinear
            "EventJitFPHomoLinear", "EventJitFPUniformLinear", "EventJitFPNormalLinear"]
 
 
-def _batched(fn, x):
-  """fn over the last axis of x (fn takes and returns 1-D tensors)."""
+def _batched(fn, x, batch_fn=None):
+  """fn over the last axis of x (fn takes and returns 1-D tensors); batch_fn, when given,
+  maps a (B, len) batch in one call."""
   if x.ndim == 1:
     return fn(x)
   if x.ndim == 0:
     raise ValueError("the input must have at least one dimension")
   lead = x.shape[:-1]
   flat = x.reshape(-1, x.shape[-1])
-  ys = [fn(flat[b]) for b in range(flat.shape[0])]
-  y = torch.stack(ys) if ys else torch.empty((0, 0), dtype=torch.float32, device=x.device)
+  if batch_fn is not None:
+    y = batch_fn(flat)
+  else:
+    ys = [fn(flat[b]) for b in range(flat.shape[0])]
+    y = torch.stack(ys) if ys else torch.empty((0, 0), dtype=torch.float32, device=x.device)
   return y.reshape(tuple(lead) + (y.shape[-1],))
 
 
@@ -78,9 +83,11 @@ class CSRLinear(_CSRLayer):
 
   def update(self, x):
     x = as_tensor(x, default_device())
-    return _batched(lambda v: _sparse.csrmv(self.weight, self.indices, self.indptr, v,
-                                            shape=(self.pre_num, self.post_num), transpose=self.transpose,
-                                            method=self.method), x)
+    shape = (self.pre_num, self.post_num)
+    return _batched(lambda v: _sparse.csrmv(self.weight, self.indices, self.indptr, v, shape=shape,
+                                            transpose=self.transpose, method=self.method), x,
+                    lambda b: _sparse.csrmv_batch(self.weight, self.indices, self.indptr, b, shape=shape,
+                                                  transpose=self.transpose))
 
 
 class EventCSRLinear(_CSRLayer):
@@ -88,8 +95,11 @@ class EventCSRLinear(_CSRLayer):
 
   def update(self, x):
     x = as_tensor(x, default_device())
-    return _batched(lambda v: _event.csrmv(self.weight, self.indices, self.indptr, v,
-                                           shape=(self.pre_num, self.post_num), transpose=self.transpose), x)
+    shape = (self.pre_num, self.post_num)
+    return _batched(lambda v: _event.csrmv(self.weight, self.indices, self.indptr, v, shape=shape,
+                                           transpose=self.transpose), x,
+                    lambda b: _event.csrmv_batch(self.weight, self.indices, self.indptr, b, shape=shape,
+                                                 transpose=self.transpose))
 
 
 class _JitLayer:

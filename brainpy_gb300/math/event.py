@@ -13,9 +13,10 @@ from typing import Optional, Tuple, Union
 import torch
 
 from .. import _lib
+from . import _grad
 from ._utils import as_tensor, default_device, event_type, float_data, index_type
 
-__all__ = ["csrmv", "csrmv_taichi", "info", "CSRPlan", "prepare"]
+__all__ = ["csrmv", "csrmv_taichi", "csrmv_batch", "info", "CSRPlan", "prepare"]
 
 
 class CSRPlan:
@@ -57,10 +58,11 @@ class CSRPlan:
     self._ws_bytes = L.bp_event_csrmv_planned_workspace_size(self._cref)
     self._ws = {}
 
-  def _workspace(self, stream_ptr):
+  def _workspace(self, stream_ptr, nbytes=None):
+    nbytes = self._ws_bytes if nbytes is None else nbytes
     ws = self._ws.get(stream_ptr)
-    if ws is None:
-      ws = torch.empty(max(self._ws_bytes, 1), dtype=torch.uint8, device=self.device)
+    if ws is None or ws.numel() < nbytes:
+      ws = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=self.device)
       self._ws[stream_ptr] = ws
     return ws
 
@@ -82,6 +84,46 @@ class CSRPlan:
       _lib.check(st, "event_csrmv_planned")
     return out
 
+
+  def csrmv_batch(self, events, data=None, out=None, float_rule=_lib.BP_EV_F32_POS):
+    """out (B, n): row b is csrmv(events[b]); one launch pair for the whole batch."""
+    return self._batch(events, data, out, float_rule, dense=False)
+
+  def sparse_t_batch(self, vectors, data=None, out=None):
+    """out (B, n): row b is sparse_t(vectors[b]); one launch pair for the whole batch."""
+    return self._batch(vectors, data, out, _lib.BP_EV_F32_NZ, dense=True)
+
+  def _batch(self, x, data, out, float_rule, dense):
+    m, n = self.shape
+    if x.ndim != 2 or x.shape[1] != m:
+      raise ValueError(f"Shape mismatch, batch {tuple(x.shape)} @ mat {self.shape}.")
+    x = x.contiguous()
+    if dense:
+      if x.dtype == torch.bool:
+        x = x.to(torch.float32)
+      if x.dtype != torch.float32:
+        raise TypeError(f"vector must be float32, got {x.dtype}")
+      etype, xv = _lib.BP_EV_F32_NZ, x
+    else:
+      etype, xv = event_type(x, float_rule)
+    b = int(x.shape[0])
+    if out is None:
+      out = torch.empty((b, n), dtype=torch.float32, device=self.device)
+    w = 0
+    if not self.heter:
+      w = (data if data is not None else self._one).data_ptr()
+    sp = _lib.raw_stream(self.device)
+    need = self._L.bp_event_csrmv_planned_batch_workspace_size(self._cref, b)
+    ws = self._workspace(sp, need)
+    if dense:
+      st = self._L.bp_csrmv_planned_batch(self._cref, w, xv.data_ptr(), b, out.data_ptr(), self.cluster,
+                                          ws.data_ptr(), ws.numel(), sp)
+    else:
+      st = self._L.bp_event_csrmv_planned_batch(self._cref, w, xv.data_ptr(), etype, b, out.data_ptr(),
+                                                self.cluster, ws.data_ptr(), ws.numel(), sp)
+    if st:
+      _lib.check(st, "csrmv_planned_batch")
+    return out
 
   def sparse_t(self, vector, data=None, out=None):
     """out (n) = A^T vector on this plan (sparse.csrmv, transpose=True)."""
@@ -172,7 +214,7 @@ def _check_common(data, indices, indptr, events, shape, transpose):
     raise ValueError(f"indptr should have shape ({shape[0] + 1},), got {tuple(indptr.shape)}.")
 
 
-def _event_csrmv(data, indices, indptr, events, shape, transpose, float_rule, out=None):
+def _event_csrmv(data, indices, indptr, events, shape, transpose, float_rule, out=None, use_plan=True):
   dev = events.device if isinstance(events, torch.Tensor) and events.is_cuda else default_device()
   data = float_data(data, dev)
   indices = as_tensor(indices, dev)
@@ -185,7 +227,7 @@ def _event_csrmv(data, indices, indptr, events, shape, transpose, float_rule, ou
   etype, ev = event_type(events, float_rule)
   m, n = int(shape[0]), int(shape[1])
   n_out = n if transpose else m
-  if transpose:
+  if transpose and use_plan:
     plan = _cached_plan(data, indices, indptr, (m, n))
     if plan is not None:
       return plan.csrmv(events, None if plan.heter else data, out=out, float_rule=float_rule)
@@ -210,13 +252,58 @@ def csrmv(data: Union[float, torch.Tensor], indices: torch.Tensor, indptr: torch
   length ``shape[0]`` (transpose) or ``shape[1]``.  A float event counts when it is
   ``> 0`` (the reference's CPU kernels); its value is not multiplied in.
   Returns float32 of length ``shape[1]`` (transpose) or ``shape[0]``.
+
+  Differentiable in ``data`` and in float ``events`` (reverse and forward mode) with the
+  reference's rules (brainpy/_src/math/event/_csr_matvec.py:521-551).
   """
-  return _event_csrmv(data, indices, indptr, events, shape, transpose, _lib.BP_EV_F32_POS)
+  return _dispatch(data, indices, indptr, events, shape, transpose, _lib.BP_EV_F32_POS)
 
 
 def csrmv_taichi(data, indices, indptr, events, *, shape, transpose=False):
   """``brainpy.math.event.csrmv_taichi``: as :func:`csrmv`, float events count when ``!= 0``."""
-  return _event_csrmv(data, indices, indptr, events, shape, transpose, _lib.BP_EV_F32_NZ)
+  return _dispatch(data, indices, indptr, events, shape, transpose, _lib.BP_EV_F32_NZ)
+
+
+def _dispatch(data, indices, indptr, events, shape, transpose, float_rule):
+  if _grad.wanted(data, events):
+    dev = events.device if isinstance(events, torch.Tensor) and events.is_cuda else default_device()
+    d = float_data(data, dev)
+    ev = as_tensor(events, dev)
+    return _grad.EventCSRMV.apply(d, ev, as_tensor(indices, dev), as_tensor(indptr, dev),
+                                  (int(shape[0]), int(shape[1])), bool(transpose), float_rule)
+  return _event_csrmv(data, indices, indptr, events, shape, transpose, float_rule)
+
+
+def csrmv_batch(data, indices, indptr, events, *, shape: Tuple[int, int], transpose: bool = False,
+                float_rule=_lib.BP_EV_F32_POS) -> torch.Tensor:
+  """csrmv mapped over the leading axis of a (B, len) batch of event vectors: (B, out).
+
+  The reference maps its primitive over a batch with a sequential scan of single calls
+  (brainpy/_src/math/op_register/utils.py:16-38); here a transpose product on a planned matrix
+  runs the whole batch in one launch pair (bp_event_csrmv_planned_batch), and the other
+  cases call the single-vector kernels row by row.  Rows are the single-vector results."""
+  dev = events.device if isinstance(events, torch.Tensor) and events.is_cuda else default_device()
+  events = as_tensor(events, dev)
+  if events.ndim != 2:
+    raise ValueError(f"events should be a 2D (batch, length) array, got {events.ndim}-D.")
+  m, n = int(shape[0]), int(shape[1])
+  if _grad.wanted(data, events):
+    rows = [_dispatch(data, indices, indptr, events[b], shape, transpose, float_rule) for b in range(events.shape[0])]
+    return torch.stack(rows) if rows else torch.empty((0, n if transpose else m), device=dev)
+  d = float_data(data, dev)
+  indices = as_tensor(indices, dev)
+  indptr = as_tensor(indptr, dev)
+  if transpose and events.shape[0] > 0:
+    _check_common(d, indices, indptr, events[0], shape, True)
+    if index_type(indptr, "indptr") != index_type(indices, "indices"):
+      raise ValueError("indices and indptr must have the same integer type.")
+    plan = _cached_plan(d, indices, indptr, (m, n))
+    if plan is not None:
+      return plan.csrmv_batch(events, None if plan.heter else d, float_rule=float_rule)
+  out = torch.empty((events.shape[0], n if transpose else m), dtype=torch.float32, device=dev)
+  for b in range(events.shape[0]):
+    _event_csrmv(d, indices, indptr, events[b], shape, transpose, float_rule, out=out[b])
+  return out
 
 
 def info(events: torch.Tensor):

@@ -16,6 +16,7 @@ import numpy as np
 import torch
 
 from .. import _lib
+from . import _grad
 from ._utils import as_tensor, default_device
 
 __all__ = [
@@ -114,21 +115,49 @@ def _doc(kind, event):
           f"brainpy.math.jitconn.{'event_' if event else ''}mv_prob_{kind}.")
 
 
+def _grad_mv(kind, event, vector, weight, p0, p1, conn_prob, seed, shape, transpose, outdim_parallel, taichi,
+             variant):
+  """The operator through the reference's differentiation rules (a fixed seed is drawn first,
+  so that the backward pass regenerates the same matrix)."""
+  dev = vector.device if isinstance(vector, torch.Tensor) and vector.is_cuda else default_device()
+  v = as_tensor(vector, dev)
+  if not event and v.dtype == torch.bool:
+    v = v.to(torch.float32)
+  w = None
+  if isinstance(weight, torch.Tensor) and _grad.wanted(weight):
+    if weight.numel() != 1:
+      raise ValueError("weight must be a 1D scalar.")
+    w = weight
+  elif weight is not None:
+    p0 = _scalar(weight, "weight")
+  return _grad.JitMV.apply(v, w, kind, event, p0, p1, conn_prob, _seed(seed, taichi), tuple(shape), bool(transpose),
+                           bool(outdim_parallel), taichi, variant)
+
+
 def _make(kind, event, taichi):
   """One public operator with the reference's signature for `kind`."""
   if kind == "homo":
     def op(vector, weight, conn_prob, seed: Optional[int] = None, *, shape: Tuple[int, int],
            transpose: bool = False, outdim_parallel: bool = True, variant: str = "gpu"):
+      if _grad.wanted(vector, weight):
+        return _grad_mv(kind, event, vector, weight, 0.0, 0.0, conn_prob, seed, shape, transpose, outdim_parallel,
+                        taichi, variant)
       return _mv(kind, event, vector, _scalar(weight, "weight"), 0.0, conn_prob, seed, shape, transpose,
                  outdim_parallel, taichi, variant)
   elif kind == "uniform":
     def op(vector, w_low, w_high, conn_prob, seed: Optional[int] = None, *, shape: Tuple[int, int],
            transpose: bool = False, outdim_parallel: bool = True, variant: str = "gpu"):
+      if _grad.wanted(vector):
+        return _grad_mv(kind, event, vector, None, _scalar(w_low, "w_low"), _scalar(w_high, "w_high"), conn_prob,
+                        seed, shape, transpose, outdim_parallel, taichi, variant)
       return _mv(kind, event, vector, _scalar(w_low, "w_low"), _scalar(w_high, "w_high"), conn_prob, seed, shape,
                  transpose, outdim_parallel, taichi, variant)
   else:
     def op(vector, w_mu, w_sigma, conn_prob, seed: Optional[int] = None, *, shape: Tuple[int, int],
            transpose: bool = False, outdim_parallel: bool = True, variant: str = "gpu"):
+      if _grad.wanted(vector):
+        return _grad_mv(kind, event, vector, None, _scalar(w_mu, "w_mu"), _scalar(w_sigma, "w_sigma"), conn_prob,
+                        seed, shape, transpose, outdim_parallel, taichi, variant)
       return _mv(kind, event, vector, _scalar(w_mu, "w_mu"), _scalar(w_sigma, "w_sigma"), conn_prob, seed, shape,
                  transpose, outdim_parallel, taichi, variant)
   op.__name__ = f"{'event_' if event else ''}mv_prob_{kind}{'_taichi' if taichi else ''}"

@@ -9,15 +9,16 @@ from typing import Tuple
 import torch
 
 from .. import _lib
+from . import _grad
 from . import event as _event
 from ._utils import as_tensor, default_device, float_data, index_type
 
-__all__ = ["csrmv", "csrmv_taichi", "csr_to_dense", "csr_to_coo", "coo_to_csr"]
+__all__ = ["csrmv", "csrmv_taichi", "csrmv_batch", "csr_to_dense", "csr_to_coo", "coo_to_csr"]
 
 _METHODS = ("cusparse", "scalar", "vector", "adaptive")
 
 
-def _csrmv(data, indices, indptr, vector, shape, transpose, out=None):
+def _csrmv(data, indices, indptr, vector, shape, transpose, out=None, use_plan=True):
   dev = vector.device if isinstance(vector, torch.Tensor) and vector.is_cuda else default_device()
   data = float_data(data, dev)
   indices = as_tensor(indices, dev)
@@ -41,7 +42,7 @@ def _csrmv(data, indices, indptr, vector, shape, transpose, out=None):
   itype = index_type(indices, "indices")
   if index_type(indptr, "indptr") != itype:
     raise ValueError("indices and indptr must have the same integer type.")
-  if transpose:
+  if transpose and use_plan:
     plan = _event._cached_plan(data, indices, indptr, (m, n))
     if plan is not None:
       return plan.sparse_t(vector, None if plan.heter else data, out=out)
@@ -63,12 +64,60 @@ def csrmv(data, indices, indptr, vector, *, shape: Tuple[int, int], transpose: b
   same sm_103a kernels here; an unknown method raises ValueError as in the reference."""
   if method not in _METHODS:
     raise ValueError(f"Only support methods: cusparse, scalar, vector, and adaptive. But we got {method}.")
-  return _csrmv(data, indices, indptr, vector, shape, bool(transpose))
+  return _dispatch(data, indices, indptr, vector, shape, bool(transpose))
 
 
 def csrmv_taichi(data, indices, indptr, vector, *, shape: Tuple[int, int], transpose: bool = False):
   """``brainpy.math.sparse.csrmv_taichi``."""
-  return _csrmv(data, indices, indptr, vector, shape, bool(transpose))
+  return _dispatch(data, indices, indptr, vector, shape, bool(transpose))
+
+
+def _dispatch(data, indices, indptr, vector, shape, transpose):
+  """The kernels directly, or -- when data or vector needs a gradient -- through the
+  reference's differentiation rules (brainpy/_src/math/sparse/_csr_mv.py:211-240)."""
+  if _grad.wanted(data, vector):
+    dev = vector.device if isinstance(vector, torch.Tensor) and vector.is_cuda else default_device()
+    d = float_data(data, dev)
+    v = as_tensor(vector, dev)
+    if v.dtype == torch.bool:
+      v = v.to(torch.float32)
+    return _grad.SparseCSRMV.apply(d, v, as_tensor(indices, dev), as_tensor(indptr, dev),
+                                   (int(shape[0]), int(shape[1])), transpose)
+  return _csrmv(data, indices, indptr, vector, shape, transpose)
+
+
+def csrmv_batch(data, indices, indptr, vectors, *, shape: Tuple[int, int], transpose: bool = False):
+  """csrmv mapped over the leading axis of a (B, len) batch of dense vectors: (B, out).  A
+  transpose product on a planned matrix runs the batch in one launch pair
+  (bp_csrmv_planned_batch); other cases run the single-vector kernels row by row (the
+  reference's batching rule is a sequential scan, brainpy/_src/math/op_register/utils.py:16-38)."""
+  dev = vectors.device if isinstance(vectors, torch.Tensor) and vectors.is_cuda else default_device()
+  vectors = as_tensor(vectors, dev)
+  if vectors.ndim != 2:
+    raise ValueError(f"vectors should be a 2D (batch, length) array, got {vectors.ndim}-D.")
+  if vectors.dtype == torch.bool:
+    vectors = vectors.to(torch.float32)
+  m, n = int(shape[0]), int(shape[1])
+  if _grad.wanted(data, vectors):
+    rows = [_dispatch(data, indices, indptr, vectors[b], shape, bool(transpose)) for b in range(vectors.shape[0])]
+    return torch.stack(rows) if rows else torch.empty((0, n if transpose else m), device=dev)
+  d = float_data(data, dev)
+  indices = as_tensor(indices, dev)
+  indptr = as_tensor(indptr, dev)
+  if transpose and vectors.shape[0] > 0:
+    if indptr.shape[0] != m + 1:
+      raise ValueError(f"indptr should have shape ({m + 1},), got {tuple(indptr.shape)}.")
+    if vectors.shape[1] != m:
+      raise ValueError(f"Shape mismatch, vec ({vectors.shape[1]},) and mat {tuple(shape)} with transpose=True.")
+    if d.shape[0] not in (1, indices.shape[0]):
+      raise ValueError("The size of data should be 1 or be consistent with indices.")
+    plan = _event._cached_plan(d, indices, indptr, (m, n))
+    if plan is not None:
+      return plan.sparse_t_batch(vectors, None if plan.heter else d)
+  out = torch.empty((vectors.shape[0], n if transpose else m), dtype=torch.float32, device=dev)
+  for b in range(vectors.shape[0]):
+    _csrmv(d, indices, indptr, vectors[b], shape, bool(transpose), out=out[b])
+  return out
 
 
 def csr_to_coo(indices, indptr):

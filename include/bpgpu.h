@@ -94,6 +94,16 @@ bp_status bp_csrmv(const float* data, int64_t ndata, const void* indices, const 
                    int64_t nnz, const float* vec, int64_t m, int64_t n, int32_t transpose, float* out,
                    bp_stream_t stream);
 
+/* Weight cotangent of event.csrmv / sparse.csrmv (the heterogeneous-data branch of their
+ * transpose rules, brainpy/_src/math/event/_csr_matvec.py:545-547 and
+ * brainpy/_src/math/sparse/_csr_mv.py:237-239, which build COO rows and gather):
+ *   out[j] = x[i] * y[indices[j]]  for every stored entry j of row i (nnz outputs),
+ * 0 where indices[j] is outside [0, n) or j lies outside every row.  For transpose=1,
+ * x = events or vector (length m) and y = cotangent (length n); for transpose=0 the roles swap
+ * (x = cotangent, y = vector). */
+bp_status bp_csr_sampled_outer(const float* x, const float* y, const void* indices, const void* indptr,
+                               bp_itype itype, int64_t nnz, int64_t m, int64_t n, float* out, bp_stream_t stream);
+
 /* CSR utilities (brainpy/_src/math/sparse/_utils.py:44-114): COO row ids of every stored entry
  * (same index type as indptr), and the dense (m x n, row-major) matrix with duplicates added. */
 bp_status bp_csr_to_coo(const void* indptr, bp_itype itype, int64_t m, int64_t nnz, void* rows, bp_stream_t stream);
@@ -178,6 +188,20 @@ bp_status bp_event_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, c
  * skipped; `w_homo` as for bp_event_csrmv_planned.  Workspace: bp_event_csrmv_planned_workspace_size. */
 bp_status bp_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, const float* vec, float* out,
                            int32_t cluster, void* workspace, size_t workspace_bytes, bp_stream_t stream);
+
+/* A batch of `batch` vectors (0..65535) through one plan in one launch pair -- the batched form
+ * that replaces the reference's batching rule for these primitives, a sequential lax.scan of
+ * single calls (brainpy/_src/math/op_register/utils.py:16-38, registered for event.csrmv at
+ * brainpy/_src/math/event/_csr_matvec.py:556).  `events` / `vec` hold batch rows of m
+ * (contiguous), `out` batch rows of n; row b of out is the single-vector result for row b.
+ * Workspace: bp_event_csrmv_planned_batch_workspace_size(plan, batch). */
+size_t bp_event_csrmv_planned_batch_workspace_size(const bp_csr_plan* plan, int32_t batch);
+bp_status bp_event_csrmv_planned_batch(const bp_csr_plan* plan, const float* w_homo, const void* events,
+                                       bp_etype etype, int32_t batch, float* out, int32_t cluster, void* workspace,
+                                       size_t workspace_bytes, bp_stream_t stream);
+bp_status bp_csrmv_planned_batch(const bp_csr_plan* plan, const float* w_homo, const float* vec, int32_t batch,
+                                 float* out, int32_t cluster, void* workspace, size_t workspace_bytes,
+                                 bp_stream_t stream);
 
 /* ---------------------------------------------------------------------------
  * event.csrmv with no allocation anywhere (no counterpart in the reference).

@@ -43,12 +43,13 @@ def parse():
   ap.add_argument("--no-cpu-baseline", action="store_true")
   ap.add_argument("--cpu-seconds", type=float, default=12.0)
   ap.add_argument("--workload", default="event_csrmv",
-                  choices=["event_csrmv", "coba", "batched", "jitconn_net", "serve", "sweep", "vmap"],
+                  choices=["event_csrmv", "coba", "batched", "jitconn_net", "serve", "sweep", "vmap", "stdp"],
                   help="event_csrmv (headline); coba: the 4000-neuron COBA example; batched: 256 uneven "
                        "networks in persistent cluster launches vs the plain per-network path; jitconn_net: "
                        "4M-neuron just-in-time network; serve: continuous-batching serving loop; sweep: the "
                        "operator sweep (event/sparse csrmv, jitconn) as one JSON line; vmap: a batch of 8 "
-                       "spike vectors through one matrix in one launch pair vs 8 sequential calls")
+                       "spike vectors through one matrix in one launch pair vs 8 sequential calls; stdp: the "
+                       "CSR layers' pre/post-spike weight updates")
   ap.add_argument("--nets", type=int, default=256)
   ap.add_argument("--sim-steps", type=int, default=0, help="override the workload's number of steps")
   return ap.parse_args()
@@ -196,7 +197,7 @@ def main():
   args = parse()
   if args.workload != "event_csrmv":
     fn = {"coba": bench_coba, "batched": bench_batched, "jitconn_net": bench_jitconn_net, "serve": bench_serve,
-          "sweep": bench_sweep, "vmap": bench_vmap}
+          "sweep": bench_sweep, "vmap": bench_vmap, "stdp": bench_stdp}
     line = fn[args.workload](args)
     if line is not None:
       print(json.dumps(line))
@@ -646,6 +647,39 @@ def bench_vmap(args, batch=8):
                      "l2": "flushed before each replay", "timing": "CUDA-graph replay, CUDA events"},
           "sequential_calls": {"value": e / t_s, "ms_per_step": t_s * 1e3},
           "speedup_vs_sequential": t_s / t_b, "gpu_launches": 2}
+
+
+def bench_stdp(args):
+  """STDP weight updates on CSR (brainpy/_src/dnn/linear.py:650-698) at N = 1e6, K = 1000:
+  the on-pre update of 2 % spiking rows, in place (what _CSRLayer.stdp_update needs), and the
+  functional form that first copies all nnz weights, as the reference's kernel does.
+  Algorithmic bytes of the in-place update: the spike vector (1 B/row), an indptr pair per
+  spiking row, and per synapse of a spiking row its int32 index, the weight read and written
+  and the float32 trace gathered (16 B)."""
+  from brainpy_gb300 import dnn
+  from brainpy_gb300.connect import bernoulli_events, fixed_prob_csr
+  n, k = args.n, args.fanout
+  ind, ptr = fixed_prob_csr(n, n, k, seed=0)
+  w = torch.full((ind.numel(),), 0.5, device="cuda")
+  w2 = torch.empty_like(w)
+  sp = bernoulli_events(n, args.rate, seed=2)
+  trace = torch.randn(n, device="cuda") * 1e-3
+  active = int(sp.sum())
+  flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+  t_in = _graph_time(lambda: dnn.csr_on_pre_update(w, ind, ptr, sp, trace, 0.0, 1.0, out=w), flush_buf)
+  t_copy = _graph_time(lambda: dnn.csr_on_pre_update(w, ind, ptr, sp, trace, 0.0, 1.0, out=w2), flush_buf)
+  peak, _ = load_peaks()
+  b = n + 8 * active + 16 * active * k
+  return {"metric": "STDP on-pre weight update (synapses updated/s)", "value": active * k / t_in,
+          "unit": "synapses/s", "n_gpus": 1, "steps": 20, "warmup": 3, "ms_per_step": t_in * 1e3,
+          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+          "config": {"workload": f"csr_on_pre_update N={n} K={k} rate={args.rate}, in place",
+                     "l2": "flushed before each replay", "timing": "CUDA-graph replay, CUDA events"},
+          "roofline": {"bound": "hbm", "achieved": b / t_in / 1e9, "peak": peak, "unit": "GB/s",
+                       "frac": b / t_in / 1e9 / peak, "alg_bytes_per_launch": b},
+          "functional_copy": {"ms_per_step": t_copy * 1e3, "value": active * k / t_copy,
+                              "note": "copies all nnz weights first, as the reference's kernel returns a new array"},
+          "gpu_launches": 1}
 
 
 def launches_per_step(args):

@@ -39,6 +39,11 @@ SIGNATURES = {
     "bp_csrmv": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_ptr, _c_i64, _c_i64, _c_i32, _c_ptr,
                           _c_ptr]),
     "bp_csr_to_coo": (_c_i32, [_c_ptr, _c_i32, _c_i64, _c_i64, _c_ptr, _c_ptr]),
+    "bp_stdp_workspace_size": (_c_size, [_c_i64]),
+    "bp_csr_on_pre_update": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_ptr, _c_i32,
+                                      _c_ptr, _c_f32, _c_f32, _c_ptr, _c_size, _c_ptr]),
+    "bp_csc_on_post_update": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_ptr,
+                                       _c_i32, _c_ptr, _c_f32, _c_f32, _c_ptr, _c_size, _c_ptr]),
     "bp_csr_sampled_outer": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_ptr,
                                       _c_ptr]),
     "bp_csr_to_dense": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_ptr, _c_ptr]),

@@ -57,6 +57,22 @@ def fixed_prob_csr(num_pre, num_post, fan_out, seed=0, device=None, index_dtype=
   return indices, indptr
 
 
+def csr2csc(indices, indptr, post_num):
+  """(pre_ids, indptr, w_ids) of the CSC form of a CSR connection, as
+  brainpy/_src/connect/base.py:645-726 with data = arange(nnz): entries sorted by column,
+  row order kept within a column; pre_ids are the rows, w_ids the CSR positions.  A one-time
+  setup conversion (the COO rows from bp_csr_to_coo, then torch's stable sort)."""
+  from .math.sparse import csr_to_coo
+  rows, cols = csr_to_coo(indices, indptr)
+  order = torch.sort(cols.to(torch.int64), stable=True).indices
+  dt = indices.dtype
+  pre_ids = rows[order].to(dt)
+  counts = torch.bincount(cols.to(torch.int64), minlength=int(post_num))[:int(post_num)]
+  c_indptr = torch.zeros(int(post_num) + 1, dtype=torch.int64, device=indices.device)
+  c_indptr[1:] = torch.cumsum(counts, 0)
+  return pre_ids, c_indptr.to(dt), order.to(dt)
+
+
 def _hash_u01(n, seed, device):
   """Counter-based uniforms in [0, 1) (float64), identical on every device."""
   i = torch.arange(n, device=device, dtype=torch.int64)

@@ -76,4 +76,9 @@ __global__ void __launch_bounds__(256) compact_unordered_kernel(const void* __re
   }
 }
 
+// Host side (event_csrmv.cu): launches compact_unordered_kernel for the event type; *count must
+// be zero on entry.
+bp_status compact_events(const void* events, bp_etype et, int64_t m, int32_t* list, int32_t* count,
+                         cudaStream_t st);
+
 }  // namespace bp

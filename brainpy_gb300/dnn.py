@@ -18,10 +18,12 @@ import torch
 from .math import event as _event
 from .math import jitconn as _jitconn
 from .math import sparse as _sparse
-from .math._utils import as_tensor, default_device
+from . import _lib
+from .math._utils import as_tensor, default_device, index_type
 
 __all__ = ["CSRLinear", "EventCSRLinear", "JitFPHomoLinear", "JitFPUniformLinear", "JitFPNormalLinear",
-           "EventJitFPHomoLinear", "EventJitFPUniformLinear", "EventJitFPNormalLinear"]
+           "EventJitFPHomoLinear", "EventJitFPUniformLinear", "EventJitFPNormalLinear",
+           "csr_on_pre_update", "csc_on_post_update"]
 
 
 def _batched(fn, x, batch_fn=None):
@@ -39,6 +41,92 @@ def _batched(fn, x, batch_fn=None):
     ys = [fn(flat[b]) for b in range(flat.shape[0])]
     y = torch.stack(ys) if ys else torch.empty((0, 0), dtype=torch.float32, device=x.device)
   return y.reshape(tuple(lead) + (y.shape[-1],))
+
+
+def _spike_arg(spike, dev):
+  sp = as_tensor(spike, dev)
+  if sp.dtype == torch.bool:
+    return _lib.BP_EV_BOOL, sp.view(torch.uint8)
+  if sp.dtype != torch.float32:
+    sp = sp.to(torch.float32)
+  return _lib.BP_EV_F32_NZ, sp
+
+
+def _bounds(w_min, w_max):
+  return (-np.inf if w_min is None else float(w_min)), (np.inf if w_max is None else float(w_max))
+
+
+_STDP_WS = {}
+
+
+def _stdp_workspace(rows, dev):
+  """One compaction workspace per (device, stream), grown on demand; calls on one stream are
+  ordered, so they can share it."""
+  key = (dev.index, _lib.raw_stream(dev))
+  need = _lib.lib().bp_stdp_workspace_size(rows)
+  ws = _STDP_WS.get(key)
+  if ws is None or ws.numel() < need:
+    ws = torch.empty(need, dtype=torch.uint8, device=dev)
+    _STDP_WS[key] = ws
+  return ws
+
+
+def _plastic(name, w, out, spike, trace, w_min, w_max, rows, call):
+  dev = w.device if isinstance(w, torch.Tensor) and w.is_cuda else default_device()
+  w = as_tensor(w, dev)
+  if w.dtype != torch.float32 or w.ndim != 1:
+    raise ValueError(f"{name}: the weight must be a 1D float32 array, got {w.dtype} {tuple(w.shape)}")
+  if out is None:
+    out = torch.empty_like(w)
+  et, sp = _spike_arg(spike, dev)
+  tr = as_tensor(trace, dev, dtype=torch.float32)
+  lo, hi = _bounds(w_min, w_max)
+  ws = _stdp_workspace(rows, dev)
+  st = call(w, out, sp, et, tr, lo, hi, ws, _lib.stream_handle(dev))
+  _lib.check(st, name)
+  return out
+
+
+def csr_on_pre_update(w, indices, indptr, spike, trace, w_min=None, w_max=None, *, out=None):
+  """brainpy/_src/dnn/linear.py:666-671: a new weight array where every synapse k of a
+  spiking pre-synaptic row becomes clip(w[k] + trace[post(k)], w_min, w_max).  ``out=w``
+  updates in place."""
+  dev = w.device if isinstance(w, torch.Tensor) and w.is_cuda else default_device()
+  ind = as_tensor(indices, dev)
+  ptr = as_tensor(indptr, dev)
+  it = index_type(ind, "indices")
+  if index_type(ptr, "indptr") != it:
+    raise ValueError("indices and indptr must have the same integer type.")
+  m = ptr.shape[0] - 1
+  n = int(trace.shape[0])
+  if spike.shape[0] != m:
+    raise ValueError(f"spike has {spike.shape[0]} entries, the CSR has {m} rows")
+  return _plastic("csr_on_pre_update", w, out, spike, trace, w_min, w_max, m,
+                  lambda w_, o, sp, et, tr, lo, hi, ws, s: _lib.lib().bp_csr_on_pre_update(
+                      _lib.ptr(w_), _lib.ptr(o), _lib.ptr(ind), _lib.ptr(ptr), it, ind.shape[0], m, n, _lib.ptr(sp),
+                      et, _lib.ptr(tr), lo, hi, _lib.ptr(ws), ws.numel(), s))
+
+
+def csc_on_post_update(w, post_ids, indptr, w_ids, spike, trace, w_min=None, w_max=None, *, out=None):
+  """brainpy/_src/dnn/linear.py:691-696: a new weight array where, for every spiking
+  post-synaptic column, each of its synapses w_ids[k] becomes clip(w + trace[post_ids[k]]);
+  (post_ids, indptr, w_ids) is the CSC form from ``connect.csr2csc`` (post_ids hold the
+  pre-synaptic ids, as in the reference).  ``out=w`` updates in place."""
+  dev = w.device if isinstance(w, torch.Tensor) and w.is_cuda else default_device()
+  pid = as_tensor(post_ids, dev)
+  ptr = as_tensor(indptr, dev)
+  wid = as_tensor(w_ids, dev)
+  it = index_type(pid, "post_ids")
+  if index_type(ptr, "indptr") != it or index_type(wid, "w_ids") != it:
+    raise ValueError("post_ids, indptr and w_ids must have the same integer type.")
+  n = ptr.shape[0] - 1
+  m = int(trace.shape[0])
+  if spike.shape[0] != n:
+    raise ValueError(f"spike has {spike.shape[0]} entries, the CSC has {n} columns")
+  return _plastic("csc_on_post_update", w, out, spike, trace, w_min, w_max, n,
+                  lambda w_, o, sp, et, tr, lo, hi, ws, s: _lib.lib().bp_csc_on_post_update(
+                      _lib.ptr(w_), _lib.ptr(o), _lib.ptr(pid), _lib.ptr(ptr), _lib.ptr(wid), it, pid.shape[0], n, m,
+                      _lib.ptr(sp), et, _lib.ptr(tr), lo, hi, _lib.ptr(ws), ws.numel(), s))
 
 
 class _CSRLayer:
@@ -71,6 +159,27 @@ class _CSRLayer:
 
   def __call__(self, x):
     return self.update(x)
+
+  def stdp_update(self, on_pre=None, on_post=None, w_min=None, w_max=None):
+    """brainpy/_src/dnn/linear.py:517-543: weight updates on pre-synaptic spikes
+    (``on_pre={'spike', 'trace'}``, trace over the post population) and on post-synaptic
+    spikes (``on_post``, trace over the pre population).  The weight is updated in place and
+    only on the spiking rows/columns; the CSC form is built once, on first use."""
+    if not isinstance(self.weight, torch.Tensor):
+      raise ValueError("When using STDP to update synaptic weights, the weight cannot be a scalar.")
+    if tuple(self.weight.shape) != tuple(self.indices.shape):
+      raise ValueError(f"The shape of weight should be the same as the shape of sparse weight "
+                       f"{tuple(self.weight.shape)}.")
+    with torch.no_grad():
+      w = self.weight
+      if on_pre is not None:
+        csr_on_pre_update(w, self.indices, self.indptr, on_pre["spike"], on_pre["trace"], w_min, w_max, out=w)
+      if on_post is not None:
+        if not hasattr(self, "_csc"):
+          from .connect import csr2csc
+          self._csc = csr2csc(self.indices, self.indptr, self.post_num)
+        pre_ids, c_indptr, w_ids = self._csc
+        csc_on_post_update(w, pre_ids, c_indptr, w_ids, on_post["spike"], on_post["trace"], w_min, w_max, out=w)
 
 
 class CSRLinear(_CSRLayer):

@@ -104,6 +104,28 @@ bp_status bp_csrmv(const float* data, int64_t ndata, const void* indices, const 
 bp_status bp_csr_sampled_outer(const float* x, const float* y, const void* indices, const void* indptr,
                                bp_itype itype, int64_t nnz, int64_t m, int64_t n, float* out, bp_stream_t stream);
 
+/* STDP weight updates of the CSR layers (brainpy/_src/dnn/linear.py:650-698, the numba targets
+ * _cpu_csr_on_pre_update / _cpu_csc_on_pre_update behind csr_on_pre_update and
+ * csc_on_post_update, called from _CSRLayer.stdp_update :517-543).
+ *   on_pre:  for every row i with spike[i] (bool, or float != 0) and every synapse k of row i,
+ *            w[k] = min(max(w[k] + trace[indices[k]], w_min), w_max)   (trace: length n)
+ *   on_post: for every column i with spike[i] and every CSC entry k of column i,
+ *            w[w_ids[k]] = min(max(w[w_ids[k]] + trace[pre_ids[k]], w_min), w_max)   (trace: length m)
+ * (pre_ids, indptr, w_ids) is the CSC form of csr2csc (connect/base.py:645-726), n columns,
+ * m rows.  w_out receives the result; w_out == w_in updates in place (event-driven: only the
+ * spiking rows are touched), otherwise w_in is copied first, as the reference returns a new
+ * array.  NaN propagates through the clip as in numpy.  Workspace: bp_stdp_workspace_size(m)
+ * bytes for on_pre, bp_stdp_workspace_size(n) for on_post (the compacted spike list). */
+size_t bp_stdp_workspace_size(int64_t rows);
+bp_status bp_csr_on_pre_update(const float* w_in, float* w_out, const void* indices, const void* indptr,
+                               bp_itype itype, int64_t nnz, int64_t m, int64_t n, const void* spike, bp_etype etype,
+                               const float* trace, float w_min, float w_max, void* workspace, size_t workspace_bytes,
+                               bp_stream_t stream);
+bp_status bp_csc_on_post_update(const float* w_in, float* w_out, const void* pre_ids, const void* indptr,
+                                const void* w_ids, bp_itype itype, int64_t nnz, int64_t n, int64_t m,
+                                const void* spike, bp_etype etype, const float* trace, float w_min, float w_max,
+                                void* workspace, size_t workspace_bytes, bp_stream_t stream);
+
 /* CSR utilities (brainpy/_src/math/sparse/_utils.py:44-114): COO row ids of every stored entry
  * (same index type as indptr), and the dense (m x n, row-major) matrix with duplicates added. */
 bp_status bp_csr_to_coo(const void* indptr, bp_itype itype, int64_t m, int64_t nnz, void* rows, bp_stream_t stream);

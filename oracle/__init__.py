@@ -56,6 +56,9 @@ def lib():
         "orc_event_csrmv": (None, [_P, _I64, _P, _P, _I32, _P, _I32, _I64, _I64, _I32, _P, _P, _P, _P]),
         "orc_csrmv": (None, [_P, _I64, _P, _P, _I32, _P, _I64, _I64, _I32, _P, _P, _P]),
         "orc_event_info": (_I64, [_P, _I64, _P]),
+        "orc_csr_on_pre_update": (None, [_P, _P, _P, _I32, _I64, _P, _P, _F32, _F32, _I64, _P]),
+        "orc_csc_on_post_update": (None, [_P, _P, _P, _P, _I32, _I64, _P, _P, _F32, _F32, _I64, _P]),
+        "orc_csr2csc": (None, [_P, _P, _I32, _I64, _I64, _P, _P, _P]),
         "orc_lif_step": (None, [_P, _I64, _P, _P, _P, _P, _P, _P, _P, _I32, _F32, _I32]),
         "orc_coba_net_run": (None, [_P, _I64, _I64, _P, _P, _F32, _P, _P, _F32, _P, _P, _P, _P, _P, _I32, _I32,
                                     _F32, _I32, _P, _I32, _P]),
@@ -166,6 +169,52 @@ def csrmv(data, indices, indptr, vec, shape, transpose):
   lib().orc_csrmv(_p(data), data.shape[0], _p(indices), _p(indptr), idx64, _p(vec), m, n, int(transpose),
                   _p(o64), _p(a64), _p(o32))
   return {"out64": o64, "abs64": a64, "out32": o32}
+
+
+def _idx(a):
+  it = np.int64 if a.dtype == np.int64 else np.int32
+  return np.ascontiguousarray(a.astype(it)), 1 if it == np.int64 else 0
+
+
+def csr_on_pre_update(w, indices, indptr, spike, trace, w_min=-np.inf, w_max=np.inf):
+  """brainpy/_src/dnn/linear.py:650-671 (numba loop): a new weight array."""
+  w = np.ascontiguousarray(w, np.float32)
+  ind, i64 = _idx(indices)
+  ptr, _ = _idx(indptr.astype(ind.dtype))
+  sp = np.ascontiguousarray(np.asarray(spike) != 0).view(np.uint8)
+  tr = np.ascontiguousarray(trace, np.float32)
+  out = np.empty_like(w)
+  lib().orc_csr_on_pre_update(_p(w), _p(ind), _p(ptr), i64, ptr.shape[0] - 1, _p(sp), _p(tr), w_min, w_max,
+                              w.shape[0], _p(out))
+  return out
+
+
+def csc_on_post_update(w, pre_ids, indptr, w_ids, spike, trace, w_min=-np.inf, w_max=np.inf):
+  """brainpy/_src/dnn/linear.py:675-696 (numba loop): a new weight array."""
+  w = np.ascontiguousarray(w, np.float32)
+  pid, i64 = _idx(pre_ids)
+  it = pid.dtype
+  ptr = np.ascontiguousarray(indptr.astype(it))
+  wid = np.ascontiguousarray(w_ids.astype(it))
+  sp = np.ascontiguousarray(np.asarray(spike) != 0).view(np.uint8)
+  tr = np.ascontiguousarray(trace, np.float32)
+  out = np.empty_like(w)
+  lib().orc_csc_on_post_update(_p(w), _p(pid), _p(ptr), _p(wid), i64, ptr.shape[0] - 1, _p(sp), _p(tr), w_min,
+                               w_max, w.shape[0], _p(out))
+  return out
+
+
+def csr2csc(indices, indptr, n):
+  """(pre_ids, indptr, w_ids) of brainpy/_src/connect/base.py:645-726 with data = arange(nnz)."""
+  ind, i64 = _idx(indices)
+  ptr = np.ascontiguousarray(indptr.astype(ind.dtype))
+  m = ptr.shape[0] - 1
+  nnz = int(ptr[-1]) if m >= 0 and ptr.size else 0
+  pre = np.zeros(nnz, np.int64)
+  cptr = np.zeros(n + 1, np.int64)
+  wid = np.zeros(nnz, np.int64)
+  lib().orc_csr2csc(_p(ind), _p(ptr), i64, m, n, _p(pre), _p(cptr), _p(wid))
+  return pre, cptr, wid
 
 
 def event_info(events):

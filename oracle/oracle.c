@@ -347,6 +347,68 @@ int64_t orc_event_info(const uint8_t* events, int64_t n, int32_t* ids) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* Plasticity on CSR / CSC (brainpy/_src/dnn/linear.py:650-698)              */
+/* ------------------------------------------------------------------------ */
+
+/* np.minimum(np.maximum(x, lo), hi): NaN stays NaN. */
+static float clip_np(float x, float lo, float hi) {
+  if (x < lo) x = lo;
+  if (x > hi) x = hi;
+  return x;
+}
+
+/* _cpu_csr_on_pre_update (linear.py:650-660): out = w; for every pre row i with spike[i],
+ * out[k] = clip(out[k] + trace[indices[k]]) over the row's synapses k. */
+void orc_csr_on_pre_update(const float* w, const void* indices, const void* indptr, int32_t idx64,
+                           int64_t m, const uint8_t* spike, const float* trace, float w_min, float w_max,
+                           int64_t nnz, float* out) {
+  memcpy(out, w, sizeof(float) * (size_t)nnz);
+  for (int64_t i = 0; i < m; ++i) {
+    if (!spike[i]) continue;
+    int64_t b = ld_idx(indptr, idx64, i), e = ld_idx(indptr, idx64, i + 1);
+    for (int64_t k = b; k < e; ++k) out[k] = clip_np(out[k] + trace[ld_idx(indices, idx64, k)], w_min, w_max);
+  }
+}
+
+/* _cpu_csc_on_pre_update (linear.py:675-686): out = w; for every post column i with spike[i],
+ * out[w_ids[k]] = clip(out[w_ids[k]] + trace[pre_ids[k]]) over the column's entries k. */
+void orc_csc_on_post_update(const float* w, const void* pre_ids, const void* indptr, const void* w_ids,
+                            int32_t idx64, int64_t n, const uint8_t* spike, const float* trace, float w_min,
+                            float w_max, int64_t nnz, float* out) {
+  memcpy(out, w, sizeof(float) * (size_t)nnz);
+  for (int64_t i = 0; i < n; ++i) {
+    if (!spike[i]) continue;
+    int64_t b = ld_idx(indptr, idx64, i), e = ld_idx(indptr, idx64, i + 1);
+    for (int64_t k = b; k < e; ++k) {
+      int64_t l = ld_idx(w_ids, idx64, k);
+      out[l] = clip_np(out[l] + trace[ld_idx(pre_ids, idx64, k)], w_min, w_max);
+    }
+  }
+}
+
+/* csr2csc (brainpy/_src/connect/base.py:645-726) with data = arange(nnz): entries sorted by
+ * column, stably (row order kept within a column).  Counting sort; outputs int64. */
+void orc_csr2csc(const void* indices, const void* indptr, int32_t idx64, int64_t m, int64_t n,
+                 int64_t* pre_ids, int64_t* c_indptr, int64_t* w_ids) {
+  memset(c_indptr, 0, sizeof(int64_t) * (size_t)(n + 1));
+  int64_t nnz = ld_idx(indptr, idx64, m);
+  for (int64_t k = 0; k < nnz; ++k) c_indptr[ld_idx(indices, idx64, k) + 1]++;
+  for (int64_t c = 0; c < n; ++c) c_indptr[c + 1] += c_indptr[c];
+  int64_t* cur = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n > 0 ? n : 1));
+  memcpy(cur, c_indptr, sizeof(int64_t) * (size_t)n);
+  for (int64_t i = 0; i < m; ++i) {
+    int64_t b = ld_idx(indptr, idx64, i), e = ld_idx(indptr, idx64, i + 1);
+    for (int64_t k = b; k < e; ++k) {
+      int64_t c = ld_idx(indices, idx64, k);
+      int64_t p = cur[c]++;
+      pre_ids[p] = i;
+      w_ids[p] = k;
+    }
+  }
+  free(cur);
+}
+
+/* ------------------------------------------------------------------------ */
 /* LIF / Expon / COBA                                                        */
 /* ------------------------------------------------------------------------ */
 

@@ -64,6 +64,16 @@ void orc_csrmv(const float* data, int64_t ndata, const void* indices, const void
 /* ---- event.info (brainpy/_src/math/event/_info_collection.py:144-155) ---- */
 int64_t orc_event_info(const uint8_t* events, int64_t n, int32_t* ids);
 
+/* plasticity (brainpy/_src/dnn/linear.py:650-698) and csr2csc (connect/base.py:645-726) */
+void orc_csr_on_pre_update(const float* w, const void* indices, const void* indptr, int32_t idx64,
+                           int64_t m, const uint8_t* spike, const float* trace, float w_min, float w_max,
+                           int64_t nnz, float* out);
+void orc_csc_on_post_update(const float* w, const void* pre_ids, const void* indptr, const void* w_ids,
+                            int32_t idx64, int64_t n, const uint8_t* spike, const float* trace, float w_min,
+                            float w_max, int64_t nnz, float* out);
+void orc_csr2csc(const void* indices, const void* indptr, int32_t idx64, int64_t m, int64_t n,
+                 int64_t* pre_ids, int64_t* c_indptr, int64_t* w_ids);
+
 /* ---- LIF / Expon / COBA step ----
  * One exponential-Euler step of a population of LifRefLTC (ltc=1) or LifRef (ltc=0)
  * neurons with two Expon+COBA conductance channels (excitatory g_e, inhibitory g_i):

@@ -386,8 +386,56 @@ def gen_csr():
   return out
 
 
+def gen_plasticity():
+  """Weight updates of the CSR layers' STDP hook (brainpy/_src/dnn/linear.py:650-698) and the
+  CSR -> CSC conversion they use (brainpy/_src/connect/base.py:645-726, numpy branch with a
+  stable argsort -- the order jnp.argsort gives the jax branch)."""
+  ns = {"np": np, "numba": types.SimpleNamespace(prange=range)}
+  load_numba_functions(os.path.join(REF, "brainpy", "_src", "dnn", "linear.py"),
+                       ["_cpu_csr_on_pre_update", "_cpu_csc_on_pre_update"], ns)
+  stable_np = types.SimpleNamespace(**{k: getattr(np, k) for k in dir(np) if not k.startswith("__")})
+  stable_np.argsort = lambda a: np.argsort(a, kind="stable")
+  cns = {"onp": stable_np, "jnp": None, "bm": None, "get_idx_type": lambda: np.int32}
+  load_functions(os.path.join(REF, "brainpy", "_src", "connect", "base.py"), ["csr2csc", "csr2coo", "coo2csc"], cns)
+  rng = np.random.default_rng(20240905)
+  out = {}
+  for m, n, k in [(50, 80, 10), (200, 120, 30), (7, 500, 100), (300, 7, 3)]:
+    indices = np.concatenate([rng.permutation(n)[:k] for _ in range(m)]).astype(np.int32)
+    indptr = (np.arange(m + 1) * k).astype(np.int32)
+    w = rng.normal(0.3, 0.2, indices.size).astype(np.float32)
+    pre_ids, c_indptr, w_ids = cns["csr2csc"]((indices, indptr), n, data=np.arange(indices.size))
+    key = f"{m}x{n}"
+    out[key + "|indices"] = indices
+    out[key + "|indptr"] = indptr
+    out[key + "|w"] = w
+    out[key + "|csc_pre_ids"] = np.asarray(pre_ids, np.int32)
+    out[key + "|csc_indptr"] = np.asarray(c_indptr, np.int32)
+    out[key + "|csc_w_ids"] = np.asarray(w_ids, np.int32)
+    pre_spike = rng.random(m) < 0.3
+    post_spike = rng.random(n) < 0.3
+    post_trace = rng.normal(0.0, 0.2, n).astype(np.float32)
+    pre_trace = rng.normal(0.0, 0.2, m).astype(np.float32)
+    out[key + "|pre_spike"] = pre_spike
+    out[key + "|post_spike"] = post_spike
+    out[key + "|post_trace"] = post_trace
+    out[key + "|pre_trace"] = pre_trace
+    for bi, (lo, hi) in enumerate([(-np.inf, np.inf), (-0.1, 0.6), (0.0, 0.3)]):
+      lo32, hi32 = np.array(lo, np.float32), np.array(hi, np.float32)
+      res = np.zeros_like(w)
+      ns["_cpu_csr_on_pre_update"](w, indices, indptr, pre_spike, post_trace, lo32, hi32, res)
+      out[key + f"|on_pre|{bi}"] = res
+      res = np.zeros_like(w)
+      ns["_cpu_csc_on_pre_update"](w, out[key + "|csc_pre_ids"], out[key + "|csc_indptr"], out[key + "|csc_w_ids"],
+                                   post_spike, pre_trace, lo32, hi32, res)
+      out[key + f"|on_post|{bi}"] = res
+  return out
+
+
 def main():
   np.seterr(over="ignore")
+  pl = gen_plasticity()
+  np.savez_compressed(os.path.join(HERE, "plasticity.npz"), **pl)
+  print("plasticity:", len(pl), "arrays")
   lf = gen_lfsr()
   np.savez_compressed(os.path.join(HERE, "lfsr88.npz"), **lf)
   print("lfsr88:", len(lf), "arrays")

@@ -39,6 +39,10 @@ SIGNATURES = {
     "bp_csrmv": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_ptr, _c_i64, _c_i64, _c_i32, _c_ptr,
                           _c_ptr]),
     "bp_csr_to_coo": (_c_i32, [_c_ptr, _c_i32, _c_i64, _c_i64, _c_ptr, _c_ptr]),
+    "bp_fixed_prob_row_lengths": (_c_i32, [_c_i64, _c_i64, _c_i32, ctypes.c_uint64, _c_i32, _c_i32, _c_ptr, _c_ptr,
+                                           _c_ptr]),
+    "bp_fixed_prob_fill": (_c_i32, [_c_i64, _c_i64, _c_i32, ctypes.c_uint64, _c_i32, _c_i32, _c_ptr, _c_ptr, _c_ptr,
+                                    _c_ptr]),
     "bp_stdp_workspace_size": (_c_size, [_c_i64]),
     "bp_csr_on_pre_update": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_ptr, _c_i32,
                                       _c_ptr, _c_f32, _c_f32, _c_ptr, _c_size, _c_ptr]),

@@ -14,6 +14,7 @@ cannot be reproduced; this generator is our own:
 """
 import math
 
+import numpy as np
 import torch
 
 _M64 = (1 << 63) - 1
@@ -55,6 +56,111 @@ def fixed_prob_csr(num_pre, num_post, fan_out, seed=0, device=None, index_dtype=
     off = _mix(hr ^ (k * 0x5851F42D + 0x14057B7E)) % bw
     indices[r0 * K:r1 * K] = (kp * bw + off).reshape(-1).to(index_dtype)
   return indices, indptr
+
+
+class FixedProb:
+  """``bp.conn.FixedProb(prob, pre_ratio, include_self, allow_multi_conn, seed)`` built on the
+  GPU (brainpy/_src/connect/random_conn.py:30-128).
+
+  Every selected pre-synaptic row gets ``K = int(post_num * prob)`` post-synaptic columns:
+  distinct and uniformly random (the law of numba's ``rng.choice(post_num, K,
+  replace=False)``), or K independent uniform draws with ``allow_multi_conn``.  With
+  ``include_self=False`` the drawn diagonal entries are removed afterwards, as in the
+  reference.  ``bp_fixed_prob_fill`` generates the rows from a counter-based sequence, so the
+  same seed gives the same connectivity on every device; the reference's numba stream itself
+  cannot be reproduced.
+
+  ``pre_ratio < 1`` selects ``int(pre_num * pre_ratio)`` rows uniformly without replacement;
+  the other rows are empty.  (The reference's build_csr returns a CSR with only the selected
+  rows, in random order, which loses which pre-synaptic neuron each row belongs to.)
+  """
+
+  def __init__(self, prob, pre_ratio=1., include_self=True, allow_multi_conn=False, seed=None, device=None):
+    if not 0. <= prob <= 1.:
+      raise ValueError(f"prob must lie in [0, 1], got {prob}")
+    if not 0. <= pre_ratio <= 1.:
+      raise ValueError(f"pre_ratio must lie in [0, 1], got {pre_ratio}")
+    self.prob = float(prob)
+    self.pre_ratio = float(pre_ratio)
+    self.include_self = bool(include_self)
+    self.allow_multi_conn = bool(allow_multi_conn)
+    self.seed = int(np.random.randint(0, 2 ** 31 - 1)) if seed is None else int(seed)
+    self.device = device
+    self.pre_num = self.post_num = None
+    self._csr = None
+
+  def __repr__(self):
+    return (f"{self.__class__.__name__}(prob={self.prob}, pre_ratio={self.pre_ratio}, "
+            f"include_self={self.include_self}, allow_multi_conn={self.allow_multi_conn}, seed={self.seed})")
+
+  def __call__(self, pre_size, post_size=None):
+    post_size = pre_size if post_size is None else post_size
+    self.pre_num = int(np.prod(pre_size))
+    self.post_num = int(np.prod(post_size))
+    self._csr = None
+    return self
+
+  def _device(self):
+    return self.device if self.device is not None else torch.device("cuda", torch.cuda.current_device())
+
+  def build_csr(self):
+    """(indices, indptr), int32, on the device."""
+    from . import _lib
+    if self.pre_num is None:
+      raise ValueError("call the connector with (pre_size, post_size) first")
+    m, n = self.pre_num, self.post_num
+    if not self.include_self and m != n:
+      raise ValueError(f"We found pre_num != post_num ({m} != {n}). But `include_self` is set to True.")
+    K = int(n * self.prob)
+    dev = self._device()
+    L = _lib.lib()
+    st = _lib.stream_handle(dev)
+    mask = None
+    if self.pre_ratio < 1.:
+      n_sel = int(m * self.pre_ratio)
+      keys = _hash_u01(m, self.seed ^ 0x5DEECE66D, dev)
+      mask = torch.zeros(m, dtype=torch.uint8, device=dev)
+      if n_sel > 0:
+        mask[torch.topk(keys, n_sel, largest=False).indices] = 1
+    if mask is None and self.include_self:
+      indptr = torch.arange(m + 1, dtype=torch.int64, device=dev) * K
+    else:
+      lengths = torch.empty(m, dtype=torch.int32, device=dev)
+      _lib.check(L.bp_fixed_prob_row_lengths(m, n, K, self.seed, int(self.allow_multi_conn), int(self.include_self),
+                                             _lib.ptr(mask) if mask is not None else None, _lib.ptr(lengths), st),
+                 "fixed_prob_row_lengths")
+      if m and int(lengths.min()) < 0:
+        raise RuntimeError("FixedProb: a row overran its draw bound")
+      indptr = torch.zeros(m + 1, dtype=torch.int64, device=dev)
+      indptr[1:] = torch.cumsum(lengths.to(torch.int64), 0)
+    nnz = int(indptr[-1]) if m else 0
+    indices = torch.empty(nnz, dtype=torch.int32, device=dev)
+    _lib.check(L.bp_fixed_prob_fill(m, n, K, self.seed, int(self.allow_multi_conn), int(self.include_self),
+                                    _lib.ptr(mask) if mask is not None else None, _lib.ptr(indptr), _lib.ptr(indices),
+                                    st), "fixed_prob_fill")
+    if nnz and int(indices.min()) < 0:
+      raise RuntimeError("FixedProb: a row overran its draw bound")
+    return indices, indptr.to(torch.int32)
+
+  def build_coo(self):
+    """(pre_ids, post_ids), int32."""
+    from .math.sparse import csr_to_coo
+    indices, indptr = self.require("csr")
+    return csr_to_coo(indices, indptr)
+
+  def require(self, *structs):
+    """'csr' / 'pre2post' -> (indices, indptr); 'coo' / 'ij' -> (pre_ids, post_ids)."""
+    out = []
+    for s in structs:
+      if s in ("csr", "pre2post"):
+        if self._csr is None:
+          self._csr = self.build_csr()
+        out.append(self._csr)
+      elif s in ("coo", "ij"):
+        out.append(self.build_coo())
+      else:
+        raise ValueError(f"unsupported structure {s!r} (csr, pre2post, coo, ij)")
+    return out[0] if len(out) == 1 else tuple(out)
 
 
 def csr2csc(indices, indptr, post_num):

@@ -126,6 +126,25 @@ bp_status bp_csc_on_post_update(const float* w_in, float* w_out, const void* pre
                                 const void* spike, bp_etype etype, const float* trace, float w_min, float w_max,
                                 void* workspace, size_t workspace_bytes, bp_stream_t stream);
 
+/* FixedProb connectivity built on the device (replaces the numba loop of
+ * brainpy/_src/connect/random_conn.py:73-128, FixedProb._iii / build_csr).  Row r (rows with
+ * row_mask[r] == 0 are empty; row_mask may be NULL) takes K = int(n * prob) columns: the first K
+ * distinct values of a counter-based i.i.d. uniform sequence on [0, n) seeded by (seed, r) -- a
+ * uniformly random K-subset in random order, the law of rng.choice(n, K, replace=False) -- or,
+ * with allow_multi, the first K values (with repeats).  include_self == 0 (m == n only) removes
+ * the diagonal entries drawn, as the reference does after drawing.  K <= 16384 without
+ * allow_multi.
+ *   bp_fixed_prob_row_lengths: lengths[r] (int32; -1 flags a row whose generation overran its
+ *     draw bound, which does not happen for valid arguments).
+ *   bp_fixed_prob_fill: indices[indptr[r] .. indptr[r+1]) for every row (int32 columns), with
+ *     indptr the exclusive sum of the lengths (K * r when include_self and no mask). */
+bp_status bp_fixed_prob_row_lengths(int64_t m, int64_t n, int32_t K, uint64_t seed, int32_t allow_multi,
+                                    int32_t include_self, const uint8_t* row_mask, int32_t* lengths,
+                                    bp_stream_t stream);
+bp_status bp_fixed_prob_fill(int64_t m, int64_t n, int32_t K, uint64_t seed, int32_t allow_multi,
+                             int32_t include_self, const uint8_t* row_mask, const int64_t* indptr, int32_t* indices,
+                             bp_stream_t stream);
+
 /* CSR utilities (brainpy/_src/math/sparse/_utils.py:44-114): COO row ids of every stored entry
  * (same index type as indptr), and the dense (m x n, row-major) matrix with duplicates added. */
 bp_status bp_csr_to_coo(const void* indptr, bp_itype itype, int64_t m, int64_t nnz, void* rows, bp_stream_t stream);

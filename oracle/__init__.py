@@ -59,6 +59,7 @@ def lib():
         "orc_csr_on_pre_update": (None, [_P, _P, _P, _I32, _I64, _P, _P, _F32, _F32, _I64, _P]),
         "orc_csc_on_post_update": (None, [_P, _P, _P, _P, _I32, _I64, _P, _P, _F32, _F32, _I64, _P]),
         "orc_csr2csc": (None, [_P, _P, _I32, _I64, _I64, _P, _P, _P]),
+        "orc_fixed_prob_row": (_I64, [ctypes.c_uint64, _I64, _I64, _I32, _I32, _I32, _P]),
         "orc_lif_step": (None, [_P, _I64, _P, _P, _P, _P, _P, _P, _P, _I32, _F32, _I32]),
         "orc_coba_net_run": (None, [_P, _I64, _I64, _P, _P, _F32, _P, _P, _F32, _P, _P, _P, _P, _P, _I32, _I32,
                                     _F32, _I32, _P, _I32, _P]),
@@ -215,6 +216,16 @@ def csr2csc(indices, indptr, n):
   wid = np.zeros(nnz, np.int64)
   lib().orc_csr2csc(_p(ind), _p(ptr), i64, m, n, _p(pre), _p(cptr), _p(wid))
   return pre, cptr, wid
+
+
+def fixed_prob_rows(seed, rows, n, K, multi=False, drop_self=False):
+  """The device FixedProb generator's rows, serially: list of int32 arrays."""
+  out = []
+  buf = np.zeros(max(K, 1), np.int32)
+  for r in rows:
+    k = lib().orc_fixed_prob_row(int(seed), int(r), int(n), int(K), int(multi), int(drop_self), _p(buf))
+    out.append(buf[:k].copy())
+  return out
 
 
 def event_info(events):

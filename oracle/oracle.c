@@ -409,6 +409,43 @@ void orc_csr2csc(const void* indices, const void* indptr, int32_t idx64, int64_t
 }
 
 /* ------------------------------------------------------------------------ */
+/* FixedProb rows (the device generator's algorithm, serially)               */
+/* ------------------------------------------------------------------------ */
+
+static uint64_t orc_mix64(uint64_t x) { /* SplitMix64 finaliser (Steele et al. 2014) */
+  x ^= x >> 30;
+  x *= 0xBF58476D1CE4E5B9ull;
+  x ^= x >> 27;
+  x *= 0x94D049BB133111EBull;
+  x ^= x >> 31;
+  return x;
+}
+
+/* Row `row` of FixedProb (brainpy/_src/connect/random_conn.py:73-128 for the law): the first K
+ * distinct values (all K values with multi) of u(t) = mulhi(mix64(key + row*C1 + t*C2), n),
+ * key = (seed + 1) * golden ratio; diagonal entries removed when drop_self.  Writes the kept
+ * values in order and returns their number. */
+int64_t orc_fixed_prob_row(uint64_t seed, int64_t row, int64_t n, int32_t K, int32_t multi, int32_t drop_self,
+                           int32_t* out) {
+  const uint64_t key = (seed + 1ull) * 0x9E3779B97F4A7C15ull;
+  uint8_t* seen = multi ? NULL : (uint8_t*)calloc((size_t)(n > 0 ? n : 1), 1);
+  int64_t count = 0, kept = 0;
+  for (uint64_t t = 0; count < K; ++t) {
+    uint64_t h = orc_mix64(key + (uint64_t)row * 0xD1B54A32D192ED03ull + t * 0x8CB92BA72F3D8DD7ull);
+    uint32_t v = (uint32_t)(((unsigned __int128)h * (uint64_t)n) >> 64);
+    if (!multi) {
+      if (seen[v]) continue;
+      seen[v] = 1;
+    }
+    ++count;
+    if (drop_self && (int64_t)v == row) continue;
+    out[kept++] = (int32_t)v;
+  }
+  free(seen);
+  return kept;
+}
+
+/* ------------------------------------------------------------------------ */
 /* LIF / Expon / COBA                                                        */
 /* ------------------------------------------------------------------------ */
 

@@ -71,6 +71,8 @@ void orc_csr_on_pre_update(const float* w, const void* indices, const void* indp
 void orc_csc_on_post_update(const float* w, const void* pre_ids, const void* indptr, const void* w_ids,
                             int32_t idx64, int64_t n, const uint8_t* spike, const float* trace, float w_min,
                             float w_max, int64_t nnz, float* out);
+int64_t orc_fixed_prob_row(uint64_t seed, int64_t row, int64_t n, int32_t K, int32_t multi, int32_t drop_self,
+                           int32_t* out);
 void orc_csr2csc(const void* indices, const void* indptr, int32_t idx64, int64_t m, int64_t n,
                  int64_t* pre_ids, int64_t* c_indptr, int64_t* w_ids);
 

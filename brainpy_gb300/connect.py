@@ -1,16 +1,13 @@
-"""On-device construction of fixed-fan-out random CSR connectivity.
+"""On-device construction of FixedProb connectivity.
 
-`fixed_prob_csr` builds the shape of ``bp.conn.FixedProb(prob).require('pre2post')``
-(brainpy/_src/connect/random_conn.py:118-128: every pre-synaptic row gets exactly
-``int(num_post * prob)`` distinct post-synaptic columns, in no particular order)
-directly in HBM, from a seed.  The reference draws each row with numba's RNG, which
-cannot be reproduced; this generator is our own:
+``FixedProb`` mirrors ``bp.conn.FixedProb`` (brainpy/_src/connect/random_conn.py:30-128) and
+``fixed_prob_csr`` is its fixed-fan-out core: every pre-synaptic row gets K distinct,
+uniformly random post-synaptic columns (the law of numba's ``rng.choice(num_post, K,
+replace=False)``), generated in HBM by ``bp_fixed_prob_fill`` from a counter-based sequence
+seeded by (seed, row).  The reference's numba stream itself cannot be reproduced; its law is.
 
-* the post range is cut into K = fan-out equal strata of width ``num_post // K``;
-* row r takes one column per stratum, uniform within the stratum, from a
-  counter-based hash of (seed, r, k);
-* the strata are visited in a per-row permuted order k -> (a_r k + b_r) mod K with
-  a_r coprime to K, so a row's columns are distinct and unsorted.
+``bernoulli_events`` and ``normal_weights`` are counter-based synthetic inputs for tests and
+benchmarks.
 """
 import math
 
@@ -30,32 +27,42 @@ def _mix(x):
   return x & _M64
 
 
-def fixed_prob_csr(num_pre, num_post, fan_out, seed=0, device=None, index_dtype=torch.int32, chunk_rows=1 << 15):
-  """Returns (indices, indptr) on `device` for a num_pre x num_post CSR with exactly
-  `fan_out` distinct columns per row."""
+def _fixed_prob_device(m, n, K, seed, allow_multi, include_self, mask, dev):
+  """(indices int32, indptr int64) of the device generator."""
+  from . import _lib
+  L = _lib.lib()
+  st = _lib.stream_handle(dev)
+  if mask is None and include_self:
+    indptr = torch.arange(m + 1, dtype=torch.int64, device=dev) * K
+  else:
+    lengths = torch.empty(m, dtype=torch.int32, device=dev)
+    _lib.check(L.bp_fixed_prob_row_lengths(m, n, K, seed, int(allow_multi), int(include_self),
+                                           _lib.ptr(mask) if mask is not None else None, _lib.ptr(lengths), st),
+               "fixed_prob_row_lengths")
+    if m and int(lengths.min()) < 0:
+      raise RuntimeError("FixedProb: a row overran its draw bound")
+    indptr = torch.zeros(m + 1, dtype=torch.int64, device=dev)
+    indptr[1:] = torch.cumsum(lengths.to(torch.int64), 0)
+  nnz = int(indptr[-1]) if m else 0
+  indices = torch.empty(nnz, dtype=torch.int32, device=dev)
+  _lib.check(L.bp_fixed_prob_fill(m, n, K, seed, int(allow_multi), int(include_self),
+                                  _lib.ptr(mask) if mask is not None else None, _lib.ptr(indptr), _lib.ptr(indices), st),
+             "fixed_prob_fill")
+  if nnz and int(indices.min()) < 0:
+    raise RuntimeError("FixedProb: a row overran its draw bound")
+  return indices, indptr
+
+
+def fixed_prob_csr(num_pre, num_post, fan_out, seed=0, device=None, index_dtype=torch.int32):
+  """(indices, indptr) on `device` of a num_pre x num_post CSR whose rows hold `fan_out`
+  distinct uniformly random columns (FixedProb with K = fan_out, include_self=True)."""
   if device is None:
-    device = torch.device("cuda")
+    device = torch.device("cuda", torch.cuda.current_device())
   K = int(fan_out)
   if K < 0 or K > num_post:
     raise ValueError(f"fan_out {K} must lie in [0, num_post={num_post}]")
-  indptr = (torch.arange(num_pre + 1, device=device, dtype=torch.int64) * K).to(index_dtype)
-  if K == 0 or num_pre == 0:
-    return torch.zeros(0, dtype=index_dtype, device=device), indptr
-  bw = num_post // K
-  cands = torch.tensor([a for a in range(1, K + 1) if math.gcd(a, K) == 1], dtype=torch.int64, device=device)
-  indices = torch.empty(num_pre * K, dtype=index_dtype, device=device)
-  k = torch.arange(K, device=device, dtype=torch.int64)[None, :]
-  s = (int(seed) * 0x9E3779B1 + 0x632BE5AB) & _M64
-  for r0 in range(0, num_pre, chunk_rows):
-    r1 = min(num_pre, r0 + chunk_rows)
-    r = torch.arange(r0, r1, device=device, dtype=torch.int64)[:, None]
-    hr = _mix(r * 0x2545F491 + s)
-    a = cands[hr % cands.numel()]
-    b = _mix(hr + 0x1B873593) % K
-    kp = (a * k + b) % K
-    off = _mix(hr ^ (k * 0x5851F42D + 0x14057B7E)) % bw
-    indices[r0 * K:r1 * K] = (kp * bw + off).reshape(-1).to(index_dtype)
-  return indices, indptr
+  indices, indptr = _fixed_prob_device(int(num_pre), int(num_post), K, int(seed), False, True, None, device)
+  return indices.to(index_dtype), indptr.to(index_dtype)
 
 
 class FixedProb:
@@ -105,7 +112,6 @@ class FixedProb:
 
   def build_csr(self):
     """(indices, indptr), int32, on the device."""
-    from . import _lib
     if self.pre_num is None:
       raise ValueError("call the connector with (pre_size, post_size) first")
     m, n = self.pre_num, self.post_num
@@ -113,8 +119,6 @@ class FixedProb:
       raise ValueError(f"We found pre_num != post_num ({m} != {n}). But `include_self` is set to True.")
     K = int(n * self.prob)
     dev = self._device()
-    L = _lib.lib()
-    st = _lib.stream_handle(dev)
     mask = None
     if self.pre_ratio < 1.:
       n_sel = int(m * self.pre_ratio)
@@ -122,24 +126,7 @@ class FixedProb:
       mask = torch.zeros(m, dtype=torch.uint8, device=dev)
       if n_sel > 0:
         mask[torch.topk(keys, n_sel, largest=False).indices] = 1
-    if mask is None and self.include_self:
-      indptr = torch.arange(m + 1, dtype=torch.int64, device=dev) * K
-    else:
-      lengths = torch.empty(m, dtype=torch.int32, device=dev)
-      _lib.check(L.bp_fixed_prob_row_lengths(m, n, K, self.seed, int(self.allow_multi_conn), int(self.include_self),
-                                             _lib.ptr(mask) if mask is not None else None, _lib.ptr(lengths), st),
-                 "fixed_prob_row_lengths")
-      if m and int(lengths.min()) < 0:
-        raise RuntimeError("FixedProb: a row overran its draw bound")
-      indptr = torch.zeros(m + 1, dtype=torch.int64, device=dev)
-      indptr[1:] = torch.cumsum(lengths.to(torch.int64), 0)
-    nnz = int(indptr[-1]) if m else 0
-    indices = torch.empty(nnz, dtype=torch.int32, device=dev)
-    _lib.check(L.bp_fixed_prob_fill(m, n, K, self.seed, int(self.allow_multi_conn), int(self.include_self),
-                                    _lib.ptr(mask) if mask is not None else None, _lib.ptr(indptr), _lib.ptr(indices),
-                                    st), "fixed_prob_fill")
-    if nnz and int(indices.min()) < 0:
-      raise RuntimeError("FixedProb: a row overran its draw bound")
+    indices, indptr = _fixed_prob_device(m, n, K, self.seed, self.allow_multi_conn, self.include_self, mask, dev)
     return indices, indptr.to(torch.int32)
 
   def build_coo(self):

@@ -528,9 +528,12 @@ static bp_status launch_tiled_g(const TiledArgs& a, int R, cudaStream_t st) {
 // (lanes per segment, chunk rounds, L2 prefetch) from the mean segment length in 16-byte
 // chunks; BPGPU_TILED=G,RND,PF overrides (tuning).
 static void tiled_config(double chunks, int& G, int& RND, int& PF) {
+  // measured on FixedProb rows (uniform columns) at N = 1e6, K = 1000 (3.9 chunks a segment,
+  // lengths spread as a multinomial): G=2, RND=2 31.6 us, flat distribution 33.0, G=4, RND=2
+  // 33.3, G=4, RND=1 37.1, G=8 38.0 at 2 % events
   if (chunks <= 1.25) { G = 1; RND = 1; }
   else if (chunks <= 2.5) { G = 2; RND = 1; }
-  else if (chunks <= 5.0) { G = 4; RND = 1; }
+  else if (chunks <= 5.0) { G = 2; RND = 2; }
   else if (chunks <= 9.0) { G = 8; RND = 1; }
   else { G = 8; RND = 2; }
   PF = 0;  // measured: L2 prefetch of the next slice does not pay at 2-10 % event rates

@@ -102,7 +102,8 @@ class NetDesc(ctypes.Structure):
               ("seg_off", _c_ptr), ("idx", _c_ptr), ("we", _c_f32), ("wi", _c_f32),
               ("p", LifParams), ("V", _c_ptr), ("ge", _c_ptr), ("gi", _c_ptr), ("t_last", _c_ptr),
               ("spike", _c_ptr), ("spike_counts", _c_ptr), ("raster", _c_ptr), ("v_trace", _c_ptr),
-              ("trace_steps", _c_i32), ("step_limit", _c_i32), ("step0", _c_i32), ("reserved", _c_i32)]
+              ("trace_steps", _c_i32), ("step_limit", _c_i32), ("step0", _c_i32), ("delay_e", _c_i32),
+              ("delay_i", _c_i32), ("ring_len", _c_i32), ("ring", _c_ptr)]
 
 
 class BPError(RuntimeError):

@@ -27,6 +27,7 @@ namespace bp {
 
 constexpr int kNetTileW = 4096;
 constexpr int kNetMaxTiles = 16;
+constexpr int kNetMaxDelay = 64;  // delay steps a network may hold (spike-history slots)
 constexpr int kNetThreads = 1024;
 
 __global__ void __launch_bounds__(256) lif_step_kernel(bp_lif_params p, int64_t n, float* __restrict__ V,
@@ -52,7 +53,19 @@ struct NetSmem {
   uint32_t acc_e[kNetTileW], acc_i[kNetTileW];
   int32_t list[2][kNetTileW];
   int32_t cnt[2];
+  int32_t nnew;                                 // spikes of the step being computed
+  uint32_t ring[kNetMaxDelay][kNetTileW / 32];  // spike bits of the last L steps (step T in slot T mod L)
 };
+
+__device__ __forceinline__ int net_pos_mod(int64_t a, int L) { return (int)(((a % L) + L) % L); }
+
+// bits of word w (32 neurons from base + 32 w) that are excitatory (global index < n_exc)
+__device__ __forceinline__ uint32_t exc_bits(int base, int w, int n_exc) {
+  const int lo = base + 32 * w;
+  if (lo + 32 <= n_exc) return 0xffffffffu;
+  if (lo >= n_exc) return 0u;
+  return (1u << (n_exc - lo)) - 1u;
+}
 
 __global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_net_desc* __restrict__ descs,
                                                                      int32_t step0, int32_t steps, float dt) {
@@ -69,6 +82,22 @@ __global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_ne
   const int words = (d.n + 31) >> 5;
   const int64_t toff_stride = d.n_tiles + 1;
 
+  // Synaptic delays (VarDelay, brainpy/_src/delay.py:334-373): the excitatory rows propagate the
+  // spikes of step T - d_e, the inhibitory rows those of T - d_i (d = 0 means the previous
+  // step's spikes, the neurons' current spike state).  Spike bits of the last L steps live in
+  // S.ring (step T in slot T mod L), loaded from and stored back to d.ring ([L][ceil(n/32)]).
+  const int L = (d.ring != nullptr && d.ring_len > 0) ? min((int)d.ring_len, kNetMaxDelay) : 0;
+  const int d_e = L ? max(0, min((int)d.delay_e, L)) : 0;
+  const int d_i = L ? max(0, min((int)d.delay_i, L)) : 0;
+  const int eff_e = max(d_e, 1), eff_i = max(d_i, 1);
+  const int words_tile = tw >> 5, word0 = base >> 5;
+  const int64_t T0 = (int64_t)step0 + d.step0;  // time index of this launch's first step
+  // every word of the L slots is set (words past the tile to zero): the warps of the last
+  // 1024-neuron round of a tile narrower than a multiple of 1024 read them
+  for (int q = 0; q < L; ++q)
+    for (int w = tid; w < kNetTileW / 32; w += blockDim.x)
+      S.ring[q][w] = (w < words_tile && word0 + w < words) ? d.ring[(int64_t)q * words + word0 + w] : 0u;
+
   // load state, zero counters, initial spike list
   if (tid < 2) S.cnt[tid] = 0;
   for (int k = tid; k < tw; k += blockDim.x) {
@@ -83,8 +112,14 @@ __global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_ne
   __syncthreads();
   for (int k0 = 0; k0 < tw; k0 += blockDim.x) {
     const int k = k0 + tid;
-    const bool sp = k < nloc && d.spike[base + k];
-    const unsigned m = __ballot_sync(0xffffffffu, sp);
+    unsigned m = __ballot_sync(0xffffffffu, k < nloc && d.spike[base + k]);
+    if (L) {  // the rows' delayed spikes for step T0, restricted to this tile's neurons
+      const uint32_t em = exc_bits(base, k >> 5, d.n_exc);
+      const uint32_t me = d_e == 0 ? m : S.ring[net_pos_mod(T0 - d_e, L)][k >> 5];
+      const uint32_t mi = d_i == 0 ? m : S.ring[net_pos_mod(T0 - d_i, L)][k >> 5];
+      m = ((me & em) | (mi & ~em)) & __ballot_sync(0xffffffffu, k < nloc);
+    }
+    const bool sp = (m >> lane) & 1u;
     int pos = 0;
     if (lane == 0 && m) pos = atomicAdd(&S.cnt[0], __popc(m));
     pos = __shfl_sync(0xffffffffu, pos, 0);
@@ -136,7 +171,11 @@ __global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_ne
     __syncthreads();
     // ---- 2. neuron update
     const float t = __fmul_rn((float)(step0 + d.step0 + s), dt);
-    if (tid == 0) S.cnt[nxt] = 0;
+    const int64_t T = T0 + s;
+    if (tid == 0) {
+      S.cnt[nxt] = 0;
+      S.nnew = 0;
+    }
     __syncthreads();
     for (int k0 = 0; k0 < tw; k0 += blockDim.x) {
       const int k = k0 + tid;
@@ -157,13 +196,23 @@ __global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_ne
       const unsigned m = __ballot_sync(0xffffffffu, sp);
       if (d.raster && lane == 0 && k - lane < nloc)
         d.raster[(int64_t)s * words + ((base + k - lane) >> 5)] = m;
+      if (lane == 0 && m) atomicAdd(&S.nnew, __popc(m));
+      // the list the next step propagates: these spikes, or delayed ones from the ring
+      unsigned ml = m;
+      if (L) {
+        if (lane == 0) S.ring[net_pos_mod(T, L)][k >> 5] = m;
+        const uint32_t em = exc_bits(base, k >> 5, d.n_exc);
+        const uint32_t me = eff_e == 1 ? m : S.ring[net_pos_mod(T + 1 - eff_e, L)][k >> 5];
+        const uint32_t mi = eff_i == 1 ? m : S.ring[net_pos_mod(T + 1 - eff_i, L)][k >> 5];
+        ml = ((me & em) | (mi & ~em)) & __ballot_sync(0xffffffffu, k < nloc);
+      }
       int pos = 0;
-      if (lane == 0 && m) pos = atomicAdd(&S.cnt[nxt], __popc(m));
+      if (lane == 0 && ml) pos = atomicAdd(&S.cnt[nxt], __popc(ml));
       pos = __shfl_sync(0xffffffffu, pos, 0);
-      if (sp) S.list[nxt][pos + __popc(m & ((1u << lane) - 1u))] = k;
+      if ((ml >> lane) & 1u) S.list[nxt][pos + __popc(ml & ((1u << lane) - 1u))] = k;
     }
     __syncthreads();
-    if (tid == 0 && d.spike_counts && S.cnt[nxt]) atomicAdd(d.spike_counts + s, S.cnt[nxt]);
+    if (tid == 0 && d.spike_counts && S.nnew) atomicAdd(d.spike_counts + s, S.nnew);
     cluster.sync();
   }
 
@@ -174,10 +223,18 @@ __global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_ne
     d.ge[base + k] = S.ge[k];
     d.gi[base + k] = S.gi[k];
     d.t_last[base + k] = S.tl[k];
-    d.spike[base + k] = 0;
+    if (L) {
+      if (my_steps > 0) d.spike[base + k] = (S.ring[net_pos_mod(T0 + my_steps - 1, L)][k >> 5] >> (k & 31)) & 1u;
+    } else {
+      d.spike[base + k] = 0;
+    }
   }
+  for (int q = 0; q < L; ++q)
+    for (int w = tid; w < words_tile; w += blockDim.x)
+      if (word0 + w < words) d.ring[(int64_t)q * words + word0 + w] = S.ring[q][w];
   __syncthreads();
-  for (int j = tid; j < S.cnt[last]; j += blockDim.x) d.spike[base + S.list[last][j]] = 1;
+  if (!L)
+    for (int j = tid; j < S.cnt[last]; j += blockDim.x) d.spike[base + S.list[last][j]] = 1;
   cluster.sync();  // no CTA leaves while another may still read its lists
 }
 

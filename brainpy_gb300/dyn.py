@@ -13,6 +13,7 @@ Two execution forms:
   neuron-update kernel per step (the per-operator path), optionally captured as a CUDA graph.
 """
 import ctypes
+import math
 from dataclasses import dataclass, field
 from typing import Optional
 
@@ -23,6 +24,40 @@ from . import _lib
 from .connect import fixed_prob_csr
 from .math import event as _event
 from .math import jitconn as _jitconn
+
+
+_MAX_DELAY = 64  # spike-history steps the cluster runner holds in shared memory
+
+
+def delay_steps(delay, dt):
+  """Delay steps of a registered delay entry (brainpy/_src/delay.py:259-264): None -> 0,
+  otherwise ceil(delay / dt) in double precision."""
+  return 0 if delay is None else int(math.ceil(float(delay) / float(dt)))
+
+
+_BIT_SHIFTS = {}
+
+
+def _shifts(dev):
+  t = _BIT_SHIFTS.get(dev)
+  if t is None:
+    t = torch.arange(32, dtype=torch.int64, device=dev)
+    _BIT_SHIFTS[dev] = t
+  return t
+
+
+def _pack_bits(spike, words):
+  """bool [n] -> int32 [words], bit b of word w = spike[32 w + b]."""
+  b = torch.zeros(words * 32, dtype=torch.int64, device=spike.device)
+  b[: spike.shape[0]] = spike.to(torch.int64)
+  v = (b.view(words, 32) << _shifts(spike.device)).sum(dim=1)
+  return torch.where(v >= (1 << 31), v - (1 << 32), v).to(torch.int32)
+
+
+def _unpack_bits(words_row, n):
+  """int32 [words] -> bool [n]."""
+  v = words_row.to(torch.int64) & 0xFFFFFFFF
+  return ((v.unsqueeze(-1) >> _shifts(words_row.device)) & 1).reshape(-1)[:n].to(torch.bool)
 
 
 @dataclass
@@ -72,10 +107,16 @@ class EINetwork:
   Connectivity is either CSR (``indices``/``indptr`` over all n pre-synaptic rows and n
   post-synaptic columns: the union of E2E+E2I rows and I2E+I2I rows, homogeneous weights
   we / wi) or just-in-time (``jitconn=dict(prob=..., seeds=(s_EE, s_EI, s_IE, s_II))``, the
-  four EventJitFPHomoLinear projections of BrainPy, outdim_parallel=True)."""
+  four EventJitFPHomoLinear projections of BrainPy, outdim_parallel=True).
+
+  ``delay_e`` / ``delay_i`` (ms, or None) are the synaptic delays of the projections leaving
+  the excitatory / inhibitory group (FullProjAlignPostMg(delay=...), brainpy/_src/dyn/
+  projections/align_post.py:225-272, registered on the group's VarDelay): the rows propagate
+  the spikes of ceil(delay / dt) steps before (brainpy/_src/delay.py:259-264, :334-373); dt is
+  the step the delays are counted in."""
 
   def __init__(self, n, n_exc, *, indices=None, indptr=None, we=0.6, wi=6.7, params: Optional[LifParams] = None,
-               jitconn=None, device=None, V0=None, net_tile=None):
+               jitconn=None, device=None, V0=None, net_tile=None, delay_e=None, delay_i=None, dt=0.1):
     self.n, self.n_exc = int(n), int(n_exc)
     # neurons per CTA in the cluster runner (multiple of 64, at most bp_net_tile_width())
     self.net_tile = int(net_tile) if net_tile is not None else None
@@ -98,11 +139,19 @@ class EINetwork:
     self.t_step = 0
     self._plan = None
     self._split = None
+    # delays in steps and the spike history: step T's spike bits in ring[T mod L]
+    self.delay_dt = float(dt)
+    self.d_e, self.d_i = delay_steps(delay_e, dt), delay_steps(delay_i, dt)
+    self.ring_len = max(self.d_e, self.d_i)
+    if self.ring_len > _MAX_DELAY:
+      raise ValueError(f"delays of {self.ring_len} steps exceed the {_MAX_DELAY} steps the runner holds")
+    self.words = (self.n + 31) // 32
+    self.ring = (torch.zeros((self.ring_len, self.words), dtype=torch.int32, device=dev) if self.ring_len else None)
 
   # ---- construction helpers ---------------------------------------------------------
   @classmethod
   def fixed_prob(cls, n_exc, n_inh, prob=0.02, we=0.6, wi=6.7, seed=0, params=None, device=None, V0=None,
-                 net_tile=None):
+                 net_tile=None, delay_e=None, delay_i=None, dt=0.1):
     """COBA.py's four FixedProb(prob) projections with fan-out int(post*prob) per group,
     merged into one n x n CSR (E rows: E targets then I targets; I rows likewise)."""
     dev = device or torch.device("cuda", torch.cuda.current_device())
@@ -118,7 +167,7 @@ class EINetwork:
     indices = torch.cat(blocks).to(torch.int32)
     indptr = (torch.arange(n + 1, device=dev, dtype=torch.int64) * k_row).to(torch.int32)
     return cls(n, n_exc, indices=indices, indptr=indptr, we=we, wi=wi, params=params, device=dev, V0=V0,
-               net_tile=net_tile)
+               net_tile=net_tile, delay_e=delay_e, delay_i=delay_i, dt=dt)
 
   def reset_state(self, V, ge, gi, t_last, spike, t_step=0):
     """Overwrites the state (tensors of length n) and the time index."""
@@ -128,6 +177,8 @@ class EINetwork:
     self.t_last.copy_(t_last)
     self.spike.copy_(spike)
     self.t_step = int(t_step)
+    if self.ring is not None:
+      self.ring.zero_()  # VarDelay.reset_state: the history starts at zero
 
   def state_numpy(self):
     return {"V": self.V.cpu().numpy(), "ge": self.ge.cpu().numpy(), "gi": self.gi.cpu().numpy(),
@@ -163,6 +214,8 @@ class EINetwork:
     d.trace_steps = int(trace_steps)
     d.step_limit = int(step_limit)
     d.step0 = int(self.t_step)
+    d.delay_e, d.delay_i, d.ring_len = self.d_e, self.d_i, self.ring_len
+    d.ring = self.ring.data_ptr() if self.ring is not None else None
     return d
 
   # ---- per-operator form ------------------------------------------------------------
@@ -177,21 +230,49 @@ class EINetwork:
       self._split = (exc, inh)
     return self._split
 
-  def _propagate_ops(self):
-    """Conductance increments of one step from self.spike (per-operator path)."""
+  def _delayed_spikes(self, T):
+    """(excitatory, inhibitory) spike vectors the projections of step T read: self.spike
+    when the group has no delay, otherwise the history slot of step T - d.  T is an int or a
+    one-element device tensor (CUDA-graph replay)."""
+    ne = self.n_exc
+    out = []
+    for d, sl in ((self.d_e, slice(0, ne)), (self.d_i, slice(ne, self.n))):
+      if d == 0:
+        out.append(self.spike[sl])
+        continue
+      if isinstance(T, torch.Tensor):
+        row = self.ring.index_select(0, torch.remainder(T.to(torch.int64) - d, self.ring_len))[0]
+      else:
+        row = self.ring[(T - d) % self.ring_len]
+      out.append(_unpack_bits(row, self.n)[sl])
+    return out
+
+  def _record_spikes(self, T):
+    """Stores self.spike as step T's history slot."""
+    if self.ring is None:
+      return
+    packed = _pack_bits(self.spike, self.words)
+    if isinstance(T, torch.Tensor):
+      self.ring.index_copy_(0, torch.remainder(T.to(torch.int64), self.ring_len), packed.unsqueeze(0))
+    else:
+      self.ring[T % self.ring_len] = packed
+
+  def _propagate_ops(self, T=None):
+    """Conductance increments of one step (per-operator path): the rows' spikes of the
+    previous step, or of their group's delay before step T."""
     ne, n = self.n_exc, self.n
     if not hasattr(self, "_w_t"):
       self._w_t = (torch.full((1,), self.we, device=self.device), torch.full((1,), self.wi, device=self.device))
     w_e, w_i = self._w_t
+    se, si = (self.spike[:ne], self.spike[ne:]) if self.ring is None else self._delayed_spikes(T)
     if self.jitconn is None:
       (ie, pe), (ii, pi) = self._csr_split()
-      dge = _event.csrmv(w_e, ie, pe, self.spike[:ne], shape=(ne, n), transpose=True)
-      dgi = _event.csrmv(w_i, ii, pi, self.spike[ne:], shape=(n - ne, n), transpose=True)
+      dge = _event.csrmv(w_e, ie, pe, se, shape=(ne, n), transpose=True)
+      dgi = _event.csrmv(w_i, ii, pi, si, shape=(n - ne, n), transpose=True)
       return dge, dgi
     p, s = self.jitconn["prob"], self.jitconn["seeds"]
     odp = bool(self.jitconn.get("outdim_parallel", True))
     ni = n - ne
-    se, si = self.spike[:ne], self.spike[ne:]
     dge = torch.empty(n, device=self.device)
     dgi = torch.empty(n, device=self.device)
     # EventJitFPHomoLinear(num_in, num_out, atomic=not odp): shape=(num_out, num_in)
@@ -203,9 +284,11 @@ class EINetwork:
 
   def step_ops(self, dt, step_dev=None, offset=0):
     """One step through the per-operator path (propagation calls + neuron kernel)."""
-    dge, dgi = self._propagate_ops()
+    T = self.t_step if step_dev is None else step_dev + offset
+    dge, dgi = self._propagate_ops(T)
     if step_dev is None:
       lif_coba_step(self.params, self.V, self.ge, self.gi, self.t_last, self.spike, dge, dgi, self.t_step, dt)
+      self._record_spikes(T)
       self.t_step += 1
       return
     st = _lib.lib().bp_lif_coba_step_dev(ctypes.byref(self.params.c()), self.n, _lib.ptr(self.V), _lib.ptr(self.ge),
@@ -213,12 +296,15 @@ class EINetwork:
                                          _lib.ptr(self.spike.view(torch.uint8)), _lib.ptr(dge), _lib.ptr(dgi),
                                          _lib.ptr(step_dev), int(offset), float(dt), _lib.stream_handle(self.device))
     _lib.check(st, "lif_coba_step_dev")
+    self._record_spikes(T)
 
   def run(self, steps, dt=0.1, method="cluster", spike_counts=None, v_trace_steps=0, graph_steps=0):
     """Advances `steps` steps.  Returns (spike counts per step [steps] int32, V trace or None).
     method "cluster": one persistent launch; "ops": per-operator launches, replayed from a
     CUDA graph of `graph_steps` steps when graph_steps > 0."""
     counts = spike_counts if spike_counts is not None else torch.zeros(steps, dtype=torch.int32, device=self.device)
+    if self.ring is not None and abs(float(dt) - self.delay_dt) > 1e-12:
+      raise ValueError(f"the delays were counted in steps of dt={self.delay_dt}; run with that dt, not {dt}")
     if method == "cluster":
       trace = torch.empty((v_trace_steps, self.n), device=self.device) if v_trace_steps else None
       run_networks([self], steps, dt, spike_counts=[counts], v_traces=[trace] if trace is not None else None,

@@ -314,7 +314,15 @@ typedef struct {
   int32_t trace_steps;
   int32_t step_limit;          /* > 0: this network stops after step_limit of the launch's steps */
   int32_t step0;               /* time index of this network's first step (added to the launch's step0) */
-  int32_t reserved;
+  /* Synaptic delays (VarDelay, brainpy/_src/delay.py:334-373), in steps (ceil(delay / dt)): at
+   * step T the excitatory rows propagate the spikes of step T - delay_e, the inhibitory rows
+   * those of T - delay_i (0: the previous step's spikes, i.e. `spike`).  ring holds the spike
+   * bits of the last ring_len steps, step T in slot T mod ring_len, [ring_len][ceil(n/32)] words,
+   * zero before the first step; ring_len >= max(delay_e, delay_i), <= 64.  ring may be NULL
+   * (ring_len 0) when both delays are 0. */
+  int32_t delay_e, delay_i;
+  int32_t ring_len;
+  uint32_t* ring;
 } bp_net_desc;
 
 /* largest n_tiles (cluster size) bp_net_run accepts, and the tile width it expects */

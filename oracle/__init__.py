@@ -6,6 +6,7 @@ baseline leg of bench.py, as the checker.  The brainpy_gb300 package never
 imports it.
 """
 import ctypes
+import math
 import os
 import subprocess
 
@@ -63,6 +64,8 @@ def lib():
         "orc_lif_step": (None, [_P, _I64, _P, _P, _P, _P, _P, _P, _P, _I32, _F32, _I32]),
         "orc_coba_net_run": (None, [_P, _I64, _I64, _P, _P, _F32, _P, _P, _F32, _P, _P, _P, _P, _P, _I32, _I32,
                                     _F32, _I32, _P, _I32, _P]),
+        "orc_coba_net_run_delayed": (None, [_P, _I64, _I64, _P, _P, _F32, _P, _P, _F32, _P, _P, _P, _P, _P, _I32,
+                                            _I32, _F32, _I32, _I32, _I32, _P, _P]),
         "cpu_event_csrmv_bool": (None, [_P, _I64, _P, _P, _P, _I64, _I64, _I32, _P]),
         "cpu_event_csrmv_bool_t_batch": (_I32, [_P, _I64, _P, _P, _P, _I64, _I64, _I64, _P]),
         "cpu_num_threads": (_I32, []),
@@ -258,6 +261,28 @@ def coba_net_run(params, n, n_exc, exc_indptr, exc_indices, we, inh_indptr, inh_
                          _p(state["t_last"]), _p(state["spike"]), step0, steps, dt, int(count_mode),
                          _p(counts), trace_steps, _p(trace))
   return counts, trace
+
+
+def delay_steps(delay, dt):
+  """delay_step of brainpy/_src/delay.py:259-264: None -> 0, else ceil(delay / dt) in double."""
+  return 0 if delay is None else int(math.ceil(float(delay) / float(dt)))
+
+
+def coba_net_run_delayed(params, n, n_exc, exc_indptr, exc_indices, we, inh_indptr, inh_indices, wi, state, step0,
+                         steps, dt, d_e, d_i):
+  """The network with delay steps d_e / d_i on the excitatory / inhibitory rows (VarDelay,
+  rotating).  state additionally carries "ring" (uint8 [L, n], L = max(d_e, d_i), created
+  at zero when missing); updated in place.  Returns spike counts per step."""
+  L = max(d_e, d_i)
+  if L > 0 and state.get("ring") is None:
+    state["ring"] = np.zeros((L, n), np.uint8)
+  ring = state.get("ring") if L > 0 else None
+  counts = np.zeros(steps, np.int64)
+  lib().orc_coba_net_run_delayed(ctypes.byref(params), n, n_exc, _p(exc_indptr), _p(exc_indices), we,
+                                 _p(inh_indptr), _p(inh_indices), wi, _p(state["V"]), _p(state["ge"]),
+                                 _p(state["gi"]), _p(state["t_last"]), _p(state["spike"]), step0, steps, dt, d_e,
+                                 d_i, L, _p(ring) if ring is not None else None, _p(counts))
+  return counts
 
 
 def cpu_event_csrmv_bool(data, indices, indptr, events, shape, transpose, out=None):

@@ -587,6 +587,56 @@ void orc_coba_net_run(const orc_lif_params* p, int64_t n, int64_t n_exc,
   free(ci);
 }
 
+/* The same network with synaptic delays on the pre-synaptic groups: VarDelay in its rotating
+ * form (brainpy/_src/delay.py:334-373).  A projection with delay_step d = ceil(delay / dt)
+ * reads, at step i, target.value when d == 0 and data[(d - i - 1) mod L] otherwise; after the
+ * neurons update, the delay stores the new spikes at data[(-i - 1) mod L] (L = the longest
+ * registered delay step; data starts at zero).  d_e applies to the excitatory rows, d_i to the
+ * inhibitory rows; ring is data, L x n bytes, carried across calls; i = step0 + s. */
+static int64_t pos_mod(int64_t a, int64_t L) { return ((a % L) + L) % L; }
+
+void orc_coba_net_run_delayed(const orc_lif_params* p, int64_t n, int64_t n_exc,
+                              const int32_t* exc_indptr, const int32_t* exc_indices, float we,
+                              const int32_t* inh_indptr, const int32_t* inh_indices, float wi,
+                              float* V, float* ge, float* gi, float* t_last, uint8_t* spike,
+                              int32_t step0, int32_t steps, float dt, int32_t d_e, int32_t d_i,
+                              int32_t L, uint8_t* ring, int64_t* spike_counts) {
+  float* dge = (float*)calloc((size_t)n, sizeof(float));
+  float* dgi = (float*)calloc((size_t)n, sizeof(float));
+  int32_t* ce = (int32_t*)calloc((size_t)n, sizeof(int32_t));
+  int32_t* ci = (int32_t*)calloc((size_t)n, sizeof(int32_t));
+  for (int32_t s = 0; s < steps; ++s) {
+    const int64_t i = (int64_t)step0 + s;
+    const uint8_t* src_e = d_e == 0 ? spike : ring + pos_mod((int64_t)d_e - i - 1, L) * n;
+    const uint8_t* src_i = d_i == 0 ? spike : ring + pos_mod((int64_t)d_i - i - 1, L) * n;
+    memset(ce, 0, sizeof(int32_t) * (size_t)n);
+    memset(ci, 0, sizeof(int32_t) * (size_t)n);
+    for (int64_t r = 0; r < n_exc; ++r) {
+      if (!src_e[r]) continue;
+      for (int32_t j = exc_indptr[r]; j < exc_indptr[r + 1]; ++j) ce[exc_indices[j]] += 1;
+    }
+    for (int64_t r = 0; r < n - n_exc; ++r) {
+      if (!src_i[n_exc + r]) continue;
+      for (int32_t j = inh_indptr[r]; j < inh_indptr[r + 1]; ++j) ci[inh_indices[j]] += 1;
+    }
+    for (int64_t k = 0; k < n; ++k) {
+      dge[k] = (float)ce[k] * we;
+      dgi[k] = (float)ci[k] * wi;
+    }
+    orc_lif_step(p, n, V, ge, gi, t_last, spike, dge, dgi, (int32_t)i, dt, 0);
+    if (L > 0) memcpy(ring + pos_mod(-i - 1, L) * n, spike, (size_t)n);
+    if (spike_counts) {
+      int64_t c = 0;
+      for (int64_t k = 0; k < n; ++k) c += spike[k];
+      spike_counts[s] = c;
+    }
+  }
+  free(dge);
+  free(dgi);
+  free(ce);
+  free(ci);
+}
+
 /* the shared deterministic exp / exprel (brainpy_gb300/csrc/bp_math.h), exported for tests */
 float orc_bp_expf(float x) { return bp_expf(x); }
 float orc_bp_exprel(float x) { return bp_exprel(x); }

@@ -124,6 +124,12 @@ int32_t cpu_event_csrmv_bool_t_batch(const float* data, int64_t ndata, const int
                                      int64_t n, float* out);
 int32_t cpu_num_threads(void);
 
+void orc_coba_net_run_delayed(const orc_lif_params* p, int64_t n, int64_t n_exc,
+                              const int32_t* exc_indptr, const int32_t* exc_indices, float we,
+                              const int32_t* inh_indptr, const int32_t* inh_indices, float wi,
+                              float* V, float* ge, float* gi, float* t_last, uint8_t* spike,
+                              int32_t step0, int32_t steps, float dt, int32_t d_e, int32_t d_i,
+                              int32_t L, uint8_t* ring, int64_t* spike_counts);
 float orc_bp_expf(float x);
 float orc_bp_exprel(float x);
 

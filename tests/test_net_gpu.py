@@ -95,3 +95,47 @@ def test_continue_across_calls(dyn):
   c2, _ = a.run(40)
   cb, _ = b.run(80)
   assert torch.equal(torch.cat([c1, c2]), cb) and torch.equal(a.V, b.V)
+
+
+def _oracle_delayed(orc, net, state, steps, step0=0):
+  p = net.params
+  op = orc.lif_params(p.V_rest, p.V_th, p.V_reset, p.tau, p.tau_ref, p.R, p.tau_e, p.tau_i, p.E_e, p.E_i, p.input,
+                      p.ltc)
+  ep, ei, ip, ii = _oracle_split(net)
+  return orc.coba_net_run_delayed(op, net.n, net.n_exc, ep, ei, np.float32(net.we), ip, ii, np.float32(net.wi),
+                                  state, step0, steps, np.float32(0.1), net.d_e, net.d_i)
+
+
+@pytest.mark.parametrize("ne,ni,delays", [(3200, 800, (0.5, 0.3)), (3200, 800, (None, 1.2)),
+                                           (12000, 3000, (0.2, 0.7)), (3200, 800, (6.4, 6.4))])
+def test_delays_cluster_against_oracle(dyn, orc, ne, ni, delays):
+  """Synaptic delays on the E and I rows (VarDelay, brainpy/_src/delay.py:334-373): the
+  persistent runner, split over two calls, against the oracle's rotating delay buffer."""
+  V0 = _v0(ne + ni, seed=8)
+  net = dyn.EINetwork.fixed_prob(ne, ni, prob=0.02, seed=5, V0=V0, delay_e=delays[0], delay_i=delays[1])
+  assert (net.d_e, net.d_i) == tuple(0 if d is None else int(np.ceil(d / 0.1)) for d in delays)
+  state = net.state_numpy()
+  c1, _ = net.run(150, method="cluster")
+  c2, _ = net.run(250, method="cluster")
+  rc = _oracle_delayed(orc, net, state, 400)
+  np.testing.assert_array_equal(torch.cat([c1, c2]).cpu().numpy(), rc)
+  got = net.state_numpy()
+  for k in ("V", "ge", "gi", "t_last", "spike"):
+    np.testing.assert_array_equal(got[k], state[k], err_msg=k)
+  assert rc.sum() > 500
+
+
+def test_delays_ops_and_graph_match_cluster(dyn):
+  V0 = _v0(4000, seed=9)
+  kw = dict(delay_e=0.4, delay_i=0.9)
+  a = dyn.EINetwork.fixed_prob(3200, 800, seed=3, V0=V0, **kw)
+  b = dyn.EINetwork(a.n, a.n_exc, indices=a.indices, indptr=a.indptr, V0=V0, **kw)
+  c = dyn.EINetwork(a.n, a.n_exc, indices=a.indices, indptr=a.indptr, V0=V0, **kw)
+  ca, _ = a.run(300, method="cluster")
+  cb, _ = b.run(300, method="ops")
+  cc, _ = c.run(300, method="ops", graph_steps=40)
+  assert torch.equal(ca, cb) and torch.equal(ca, cc)
+  assert torch.equal(a.V, b.V) and torch.equal(a.V, c.V)
+  assert torch.equal(a.ring, b.ring) and torch.equal(a.ring, c.ring)
+  with pytest.raises(ValueError):
+    a.run(10, dt=0.05)

@@ -51,6 +51,8 @@ def parse():
                        "spike vectors through one matrix in one launch pair vs 8 sequential calls; stdp: the "
                        "CSR layers' pre/post-spike weight updates")
   ap.add_argument("--nets", type=int, default=256)
+  ap.add_argument("--delay", type=float, default=None,
+                  help="coba: synaptic delay (ms) of every projection, as FullProjAlignPostMg(delay=...)")
   ap.add_argument("--sim-steps", type=int, default=0, help="override the workload's number of steps")
   return ap.parse_args()
 
@@ -395,9 +397,10 @@ def bench_coba(args):
   V0 = np.random.default_rng(3).normal(-55.0, 5.0, 4000).astype(np.float32)
   net = dyn.EINetwork.fixed_prob(3200, 800, prob=0.02, seed=0, V0=V0)
   tile = int(os.environ.get("BPGPU_NET_TILE", "0")) or None
-  net2 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=V0, net_tile=tile)
+  dk = dict(delay_e=args.delay, delay_i=args.delay)
+  net2 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=V0, net_tile=tile, **dk)
   net2.run(100)  # warm-up: plan build, module load
-  net2 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=V0, net_tile=tile)
+  net2 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=V0, net_tile=tile, **dk)
   net2._cluster_plan()  # plan built outside the timed region
   clocks = ClockSampler(torch.cuda.current_device())
   counts = torch.zeros(steps, dtype=torch.int32, device="cuda")
@@ -407,16 +410,16 @@ def bench_coba(args):
   fan = 64 + 16
   # per-operator path, host loop and CUDA-graph replay, on a bounded number of steps
   k_ops = min(steps, 1000)
-  net3 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=V0)
+  net3 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=V0, **dk)
   net3.run(5, method="ops")
   t_ops, _ = _cuda_time(lambda: net3.run(k_ops, method="ops"))
-  net4 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=V0)
+  net4 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=V0, **dk)
   net4.run(60, method="ops", graph_steps=50)
   t_graph, _ = _cuda_time(lambda: net4.run(k_ops, method="ops", graph_steps=50))
   # e2e: host V0 in, spike counts out, whole run through the public API
   host_v0 = torch.from_numpy(V0).pin_memory()
   def e2e():
-    n5 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=host_v0)
+    n5 = dyn.EINetwork(net.n, net.n_exc, indices=net.indices, indptr=net.indptr, V0=host_v0, **dk)
     c, _ = n5.run(steps)
     return c.cpu()
   t_e2e, _ = _cuda_time(e2e)
@@ -434,14 +437,19 @@ def bench_coba(args):
   op = oracle.lif_params()
   k_cpu = min(steps, 2000)
   t0 = time.perf_counter()
-  oracle.coba_net_run(op, 4000, 3200, ptr[:3201].astype(np.int32), np.ascontiguousarray(ind[:e_end]),
-                      np.float32(0.6), (ptr[3200:] - e_end).astype(np.int32), np.ascontiguousarray(ind[e_end:]),
-                      np.float32(6.7), st, 0, k_cpu, np.float32(0.1))
+  csr = (ptr[:3201].astype(np.int32), np.ascontiguousarray(ind[:e_end]), np.float32(0.6),
+         (ptr[3200:] - e_end).astype(np.int32), np.ascontiguousarray(ind[e_end:]), np.float32(6.7))
+  if args.delay is None:
+    oracle.coba_net_run(op, 4000, 3200, *csr, st, 0, k_cpu, np.float32(0.1))
+  else:
+    oracle.coba_net_run_delayed(op, 4000, 3200, *csr, st, 0, k_cpu, np.float32(0.1), net2.d_e, net2.d_i)
   t_cpu = time.perf_counter() - t0
   return {"metric": "network-steps/s (COBA E/I 4000 neurons, dt 0.1 ms)", "value": steps / t_cluster,
           "unit": "steps/s", "n_gpus": 1, "steps": steps, "warmup": 100, "ms_per_step": t_cluster / steps * 1e3,
           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-          "config": {"workload": "COBA 3200E+800I FixedProb(0.02) LifRefLTC, 10000 steps", "path": "persistent cluster"},
+          "config": {"workload": "COBA 3200E+800I FixedProb(0.02) LifRefLTC, 10000 steps"
+                                 + (f", delay {args.delay} ms" if args.delay is not None else ""),
+                     "path": "persistent cluster"},
           "synaptic_events_per_s": n_spk * fan / t_cluster, "firing_rate_hz": n_spk / 4000 / (steps * 1e-4),
           "per_op_path_steps_per_s": k_ops / t_ops, "per_op_graph_steps_per_s": k_ops / t_graph,
           "e2e": {"value": steps / t_e2e, "unit": "steps/s", "h2d_bytes_per_step": 4000 * 4 / steps,

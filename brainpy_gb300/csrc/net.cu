@@ -128,6 +128,14 @@ __global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_ne
   cluster.sync();
 
   const int my_steps = d.step_limit > 0 ? min(steps, d.step_limit) : steps;
+  // history slots of step T (written) and of T + 1 - eff_e / eff_i (read for the next step's
+  // list), advanced by one each step (no division in the loop)
+  int slot_w = 0, slot_e = 0, slot_i = 0;
+  if (L) {
+    slot_w = net_pos_mod(T0, L);
+    slot_e = net_pos_mod(T0 + 1 - eff_e, L);
+    slot_i = net_pos_mod(T0 + 1 - eff_i, L);
+  }
   for (int s = 0; s < my_steps; ++s) {
     const int cur = s & 1, nxt = cur ^ 1;
     // ---- 1. propagate the previous step's spikes into this tile's counters
@@ -171,7 +179,6 @@ __global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_ne
     __syncthreads();
     // ---- 2. neuron update
     const float t = __fmul_rn((float)(step0 + d.step0 + s), dt);
-    const int64_t T = T0 + s;
     if (tid == 0) {
       S.cnt[nxt] = 0;
       S.nnew = 0;
@@ -200,10 +207,10 @@ __global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_ne
       // the list the next step propagates: these spikes, or delayed ones from the ring
       unsigned ml = m;
       if (L) {
-        if (lane == 0) S.ring[net_pos_mod(T, L)][k >> 5] = m;
+        if (lane == 0) S.ring[slot_w][k >> 5] = m;
         const uint32_t em = exc_bits(base, k >> 5, d.n_exc);
-        const uint32_t me = eff_e == 1 ? m : S.ring[net_pos_mod(T + 1 - eff_e, L)][k >> 5];
-        const uint32_t mi = eff_i == 1 ? m : S.ring[net_pos_mod(T + 1 - eff_i, L)][k >> 5];
+        const uint32_t me = eff_e == 1 ? m : S.ring[slot_e][k >> 5];
+        const uint32_t mi = eff_i == 1 ? m : S.ring[slot_i][k >> 5];
         ml = ((me & em) | (mi & ~em)) & __ballot_sync(0xffffffffu, k < nloc);
       }
       int pos = 0;
@@ -213,6 +220,11 @@ __global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_ne
     }
     __syncthreads();
     if (tid == 0 && d.spike_counts && S.nnew) atomicAdd(d.spike_counts + s, S.nnew);
+    if (L) {
+      slot_w = slot_w + 1 == L ? 0 : slot_w + 1;
+      slot_e = slot_e + 1 == L ? 0 : slot_e + 1;
+      slot_i = slot_i + 1 == L ? 0 : slot_i + 1;
+    }
     cluster.sync();
   }
 

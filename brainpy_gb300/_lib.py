@@ -56,6 +56,7 @@ SIGNATURES = {
     "bp_jitconn_dense": (_c_i32, [_c_i32, _c_f32, _c_f32, _c_i32, _c_u32, _c_i64, _c_i64, _c_i32, _c_i32, _c_ptr,
                                   _c_ptr]),
     "bp_csr_plan_default_tile": (_c_i32, [_c_i64, _c_i32]),
+    "bp_csr_plan_variants": (_c_i32, [_c_ptr, _c_i32]),
     "bp_csr_plan_bytes": (_c_size, [_c_i64, _c_i64, _c_i64, _c_i32, _c_i32]),
     "bp_csr_plan_build": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_i32, _c_ptr,
                                    _c_size, _c_ptr, _c_ptr]),
@@ -85,7 +86,7 @@ SIGNATURES = {
 class CsrPlan(ctypes.Structure):
   """Mirror of bp_csr_plan (include/bpgpu.h)."""
   _fields_ = [("m", _c_i64), ("n", _c_i64), ("nnz", _c_i64), ("tile_w", _c_i32), ("n_tiles", _c_i32),
-              ("heter", _c_i32), ("reserved", _c_i32), ("entries", ctypes.c_uint64), ("mem", _c_ptr),
+              ("heter", _c_i32), ("variant", _c_i32), ("entries", ctypes.c_uint64), ("mem", _c_ptr),
               ("bytes", _c_size)]
 
 

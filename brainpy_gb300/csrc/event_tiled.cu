@@ -200,6 +200,7 @@ struct TiledArgs {
   int64_t m, n;  // a batch of vectors: row_val rows of m, out rows of n
   int32_t tile_w, n_tiles, nb, acc_words;
   int32_t batch;    // vectors per launch: gridDim.y
+  int32_t variant;  // the plan's chosen kernel variant (0: from the segment length)
   int32_t vec_out;  // every vector's out row is 16-byte aligned (tile_w is a multiple of 4)
 };
 
@@ -525,9 +526,10 @@ static bp_status launch_tiled_g(const TiledArgs& a, int R, cudaStream_t st) {
   return BP_OK;
 }
 
-// (lanes per segment, chunk rounds, L2 prefetch) from the mean segment length in 16-byte
-// chunks; BPGPU_TILED=G,RND,PF overrides (tuning).
-static void tiled_config(double chunks, int& G, int& RND, int& PF) {
+// (lanes per segment, chunk rounds, L2 prefetch): the plan's chosen variant when set
+// (bp_csr_plan.variant = G | RND << 8 | PF << 16, e.g. from an autotuning pass), otherwise
+// from the mean segment length in 16-byte chunks; BPGPU_TILED=G,RND,PF overrides both.
+static void tiled_config(double chunks, int32_t variant, int& G, int& RND, int& PF) {
   // measured on FixedProb rows (uniform columns) at N = 1e6, K = 1000 (3.9 chunks a segment,
   // lengths spread as a multinomial): G=2, RND=2 31.6 us, flat distribution 33.0, G=4, RND=2
   // 33.3, G=4, RND=1 37.1, G=8 38.0 at 2 % events
@@ -537,6 +539,11 @@ static void tiled_config(double chunks, int& G, int& RND, int& PF) {
   else if (chunks <= 9.0) { G = 8; RND = 1; }
   else { G = 8; RND = 2; }
   PF = 0;  // measured: L2 prefetch of the next slice does not pay at 2-10 % event rates
+  if (variant > 0) {
+    G = variant & 0xFF;
+    RND = (variant >> 8) & 0xFF;
+    PF = (variant >> 16) & 1;
+  }
   static int env[3] = {-1, -1, -1};
   if (env[0] < 0) {
     env[0] = 0;
@@ -553,7 +560,7 @@ static void tiled_config(double chunks, int& G, int& RND, int& PF) {
 template <int MODE>
 static bp_status launch_tiled(const TiledArgs& a, int R, double chunks, cudaStream_t st) {
   int G, RND, PF;
-  tiled_config(chunks, G, RND, PF);
+  tiled_config(chunks, a.variant, G, RND, PF);
 #define BP_TILED_CASE(g, r)                                                                           \
   if (G == g && RND == r) {                                                                           \
     if (a.batch > 1) return launch_tiled_g<MODE, g, r, false, true>(a, R, st);                        \
@@ -628,6 +635,7 @@ static bp_status tiled_args_from_plan(const bp_csr_plan* plan, int cluster, Tile
   a.idx = v.idx;
   a.w = v.w;
   a.batch = 1;
+  a.variant = plan->variant;
   a.m = plan->m;
   a.n = plan->n;
   a.tile_w = plan->tile_w;
@@ -644,6 +652,13 @@ static bp_status tiled_args_from_plan(const bp_csr_plan* plan, int cluster, Tile
 using namespace bp;
 
 extern "C" {
+
+int32_t bp_csr_plan_variants(int32_t* codes, int32_t cap) {
+  static const int32_t kVariants[] = {1 | 1 << 8, 2 | 1 << 8, 4 | 1 << 8, 2 | 2 << 8, 8 | 1 << 8, 8 | 2 << 8};
+  const int32_t nv = (int32_t)(sizeof(kVariants) / sizeof(kVariants[0]));
+  for (int32_t i = 0; codes && i < nv && i < cap; ++i) codes[i] = kVariants[i];
+  return nv;
+}
 
 int32_t bp_csr_plan_default_tile(int64_t n, int32_t cluster) {
   if (n <= 0) return 0;

@@ -85,6 +85,47 @@ class CSRPlan:
     return out
 
 
+  @staticmethod
+  def variants():
+    """Codes of the compiled tiled-kernel variants (G | RND << 8: lanes per segment, 16-byte
+    chunks per lane and round)."""
+    L = _lib.lib()
+    k = L.bp_csr_plan_variants(None, 0)
+    buf = (ctypes.c_int32 * k)()
+    L.bp_csr_plan_variants(buf, k)
+    return list(buf)
+
+  @property
+  def variant(self):
+    """The kernel variant this plan runs (0: chosen from the mean segment length)."""
+    return int(self.c.variant)
+
+  @variant.setter
+  def variant(self, code):
+    self.c.variant = int(code)
+
+  def autotune(self, events, data=None, candidates=None, reps=10):
+    """Times every candidate variant (default: all compiled ones) on `events` -- a spike
+    vector of the rate the model runs at -- and keeps the fastest for this plan.  Returns
+    {variant code: microseconds per call}.  Every variant computes the same result."""
+    m, n = self.shape
+    out = torch.empty(n, dtype=torch.float32, device=self.device)
+    times = {}
+    for code in (candidates or self.variants()):
+      self.c.variant = int(code)
+      for _ in range(2):
+        self.csrmv(events, data, out=out)
+      t0 = torch.cuda.Event(enable_timing=True)
+      t1 = torch.cuda.Event(enable_timing=True)
+      t0.record()
+      for _ in range(reps):
+        self.csrmv(events, data, out=out)
+      t1.record()
+      t1.synchronize()
+      times[int(code)] = t0.elapsed_time(t1) * 1e3 / reps
+    self.c.variant = min(times, key=times.get)
+    return times
+
   def csrmv_batch(self, events, data=None, out=None, float_rule=_lib.BP_EV_F32_POS):
     """out (B, n): row b is csrmv(events[b]); one launch pair for the whole batch."""
     return self._batch(events, data, out, float_rule, dense=False)

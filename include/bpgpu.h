@@ -194,7 +194,9 @@ typedef struct {
   int32_t tile_w;     /* columns per tile (<= 65535) */
   int32_t n_tiles;    /* ceil(n / tile_w) */
   int32_t heter;      /* 1: the plan carries permuted float32 weights */
-  int32_t reserved;
+  int32_t variant;    /* tiled-kernel variant G | RND << 8 | PF << 16 (lanes per segment, chunk rounds,
+                         L2 prefetch), 0 = chosen from the mean segment length; set by the caller,
+                         e.g. after timing the candidates of bp_csr_plan_variants */
   uint64_t entries;   /* capacity of the padded index array */
   void* mem;          /* device memory holding the plan (caller-owned) */
   size_t bytes;       /* size of mem */
@@ -204,6 +206,9 @@ typedef struct {
  * clusters of `cluster` CTAs (1, 2, 4 or 8); 0 on error. */
 int32_t bp_csr_plan_default_tile(int64_t n, int32_t cluster);
 size_t bp_csr_plan_bytes(int64_t m, int64_t n, int64_t nnz, int32_t heter, int32_t tile_w);
+/* The compiled tiled-kernel variants (bp_csr_plan.variant codes): writes up to `cap` codes into
+ * `codes` and returns how many there are. */
+int32_t bp_csr_plan_variants(int32_t* codes, int32_t cap);
 /* Builds the plan on `stream` (heterogeneous when ndata == nnz > 1, homogeneous when
  * data is NULL or ndata == 1). */
 bp_status bp_csr_plan_build(const float* data, int64_t ndata, const void* indices, const void* indptr,

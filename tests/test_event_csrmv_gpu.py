@@ -226,3 +226,27 @@ def test_tiled_kernel_variants(bplib, orc, variant):
   r = subprocess.run([sys.executable, os.path.join(here, "_tiled_case.py")], env=env, capture_output=True, text=True,
                      timeout=600)
   assert r.returncode == 0 and r.stdout.strip().endswith("OK"), r.stdout[-2000:] + r.stderr[-4000:]
+
+
+def test_plan_autotune_and_every_variant(ev, orc):
+  """The plan's autotuner times every compiled variant and keeps the fastest; every variant
+  gives the oracle's exact counts."""
+  from brainpy_gb300.connect import fixed_prob_csr
+  n, k = 50000, 200
+  ind, ptr = fixed_prob_csr(n, n, k, seed=4)
+  ind_h, ptr_h = ind.cpu().numpy(), ptr.cpu().numpy()
+  rng = np.random.default_rng(6)
+  events = rng.random(n) < 0.05
+  plan = ev.prepare(ind, ptr, shape=(n, n))
+  w = torch.tensor([0.5], device="cuda")
+  e = torch.as_tensor(events, device="cuda")
+  times = plan.autotune(e, w, reps=3)
+  assert set(times) == set(plan.variants()) and plan.variant == min(times, key=times.get)
+  want = orc.event_csrmv(np.float32(0.5), ind_h, ptr_h, events, (n, n), True)["count32"]
+  for code in plan.variants():
+    plan.variant = code
+    np.testing.assert_array_equal(plan.csrmv(e, w).cpu().numpy(), want)
+  plan.variant = 3 | 3 << 8  # not a compiled variant
+  from brainpy_gb300 import _lib
+  with pytest.raises(_lib.BPError):
+    plan.csrmv(e, w)

@@ -76,6 +76,58 @@ __global__ void __launch_bounds__(256) jc_pull_gpu_kernel(JcArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// Taichi GPU algorithm, pull, homogeneous weight and bool events: lane-major.
+// Stream (row, l) of the algorithm above only visits columns [l * step, (l + 1) * step), so a
+// block that takes one lane index l (blockIdx.y) for a run of rows holds the event bits of
+// that range in shared memory (step / 8 bytes) and every thread walks one (row, l) stream
+// against it: no global gather per generated connection.  The homogeneous weight draws
+// nothing from the stream, so a stream contributes (number of active events it visits) * w;
+// the counts are added per row as exact integers (into `out`, reinterpreted) and turned into
+// count * w by jc_counts_to_out_kernel.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) jc_pull_homo_bool_lanes_kernel(JcArgs a, int64_t rows_per_block) {
+  extern __shared__ uint32_t ev_bits[];
+  const uint32_t l = blockIdx.y;
+  const uint32_t lim = (uint32_t)a.num_col;
+  const uint32_t c0 = a.step * l;
+  const uint32_t c1 = c0 >= lim ? c0 : (lim - c0 < a.step ? lim : c0 + a.step);
+  const uint32_t nwords = (c1 - c0 + 31u) >> 5;
+  const uint8_t* ev = static_cast<const uint8_t*>(a.vec);
+  for (uint32_t w = threadIdx.x; w < nwords; w += blockDim.x) {
+    uint32_t word = 0;
+    const uint32_t cb = c0 + 32u * w;
+#pragma unroll 8
+    for (uint32_t b = 0; b < 32u; ++b)
+      if (cb + b < c1 && ev[cb + b]) word |= 1u << b;
+    ev_bits[w] = word;
+  }
+  __syncthreads();
+  int32_t* counts = reinterpret_cast<int32_t*>(a.out);
+  const int64_t r0 = (int64_t)blockIdx.x * rows_per_block;
+  const int64_t r1 = r0 + rows_per_block < a.num_row ? r0 + rows_per_block : a.num_row;
+  for (int64_t row = r0 + threadIdx.x; row < r1; row += blockDim.x) {
+    const uint32_t i = (uint32_t)(row * 32 + l);
+    uint32_t c = c0 - 1u;
+    uint32_t end = c + a.step;
+    if (lim < end) end = lim;
+    Lfsr88 key = lfsr88_key(a.seed + i);
+    c += lfsr88_inc(key, a.fm);
+    int cnt = 0;
+    while (c < end) {  // c0 <= c < c1 here
+      const uint32_t o = c - c0;
+      cnt += (int)((ev_bits[o >> 5] >> (o & 31u)) & 1u);
+      c += lfsr88_inc(key, a.fm);
+    }
+    if (cnt) atomicAdd(counts + row, cnt);
+  }
+}
+
+__global__ void __launch_bounds__(256) jc_counts_to_out_kernel(float* __restrict__ out, int64_t n, float w) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = __fmul_rn((float)reinterpret_cast<const int32_t*>(out)[k], w);
+}
+
+// ---------------------------------------------------------------------------
 // Taichi GPU algorithm, push: warp per input column
 // ---------------------------------------------------------------------------
 template <int KIND, int VK>
@@ -218,9 +270,46 @@ static int grid_threads(int64_t owners, int max_blocks) {
   return (int)(g > max_blocks ? max_blocks : g);
 }
 
+constexpr size_t kLaneBitsMax = 200 * 1024;  // shared-memory event bits of one lane's range
+
+// the lane-major pull when the lane's column range fits shared memory
+static bp_status launch_pull_homo_bool_lanes(const JcArgs& a, cudaStream_t st, bool& done) {
+  done = false;
+  const size_t bytes = (((size_t)a.step + 31) / 32) * sizeof(uint32_t);
+  if (bytes > kLaneBitsMax) return BP_OK;
+  static bool configured[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!configured[dev]) {
+    BP_CUDA_TRY(cudaFuncSetAttribute(jc_pull_homo_bool_lanes_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kLaneBitsMax));
+    configured[dev] = true;
+  }
+  // blocks per lane: enough CTAs to fill the GPU; each loads its lane's bits once
+  int64_t per_lane = ((int64_t)device_sm_count() * 8 + 31) / 32;
+  int64_t rows_per_block = (a.num_row + per_lane - 1) / per_lane;
+  if (rows_per_block < 256) rows_per_block = 256;
+  per_lane = (a.num_row + rows_per_block - 1) / rows_per_block;
+  BP_CUDA_TRY(cudaMemsetAsync(a.out, 0, sizeof(float) * (size_t)a.num_row, st));
+  jc_pull_homo_bool_lanes_kernel<<<dim3((unsigned)per_lane, 32), 256, bytes, st>>>(a, rows_per_block);
+  bp_status s = check_launch("jc_pull_homo_bool_lanes_kernel");
+  if (s != BP_OK) return s;
+  int64_t g = (a.num_row + 255) / 256;
+  const int64_t maxb = (int64_t)device_sm_count() * 16;
+  jc_counts_to_out_kernel<<<(unsigned)(g > maxb ? maxb : g), 256, 0, st>>>(a.out, a.num_row, a.p0);
+  done = true;
+  return check_launch("jc_counts_to_out_kernel");
+}
+
 template <int KIND, int VK>
 static bp_status launch_mv(const JcArgs& a, int odp, int variant, cudaStream_t st) {
   const int maxb = device_sm_count() * 32;
+  if (KIND == JC_HOMO && VK == VEC_EV_BOOL && odp && variant == BP_JC_TAICHI_GPU) {
+    bool done = false;
+    bp_status s = launch_pull_homo_bool_lanes(a, st, done);
+    if (s != BP_OK || done) return s;
+  }
   if (variant == BP_JC_TAICHI_GPU) {
     if (odp) jc_pull_gpu_kernel<KIND, VK><<<grid_warps(a.num_row, maxb), 256, 0, st>>>(a);
     else jc_push_gpu_kernel<KIND, VK><<<grid_warps(a.num_col, maxb), 256, 0, st>>>(a);

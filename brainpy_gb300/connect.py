@@ -27,9 +27,21 @@ def _mix(x):
   return x & _M64
 
 
+def _gpu_device(device):
+  """The CUDA device the generator runs on: `device` itself, or the current CUDA device when
+  the arrays are wanted elsewhere (they are built on the GPU and copied)."""
+  if device is not None and torch.device(device).type == "cuda":
+    return torch.device(device)
+  if not torch.cuda.is_available():
+    raise RuntimeError("the FixedProb generator runs on a CUDA device (sm_103a); none is available")
+  return torch.device("cuda", torch.cuda.current_device())
+
+
 def _fixed_prob_device(m, n, K, seed, allow_multi, include_self, mask, dev):
-  """(indices int32, indptr int64) of the device generator."""
+  """(indices int32, indptr int64) of the device generator, on CUDA device `dev`."""
   from . import _lib
+  if dev.type != "cuda":
+    raise ValueError(f"the generator's arrays must live on a CUDA device, not {dev}")
   L = _lib.lib()
   st = _lib.stream_handle(dev)
   if mask is None and include_self:
@@ -56,13 +68,13 @@ def _fixed_prob_device(m, n, K, seed, allow_multi, include_self, mask, dev):
 def fixed_prob_csr(num_pre, num_post, fan_out, seed=0, device=None, index_dtype=torch.int32):
   """(indices, indptr) on `device` of a num_pre x num_post CSR whose rows hold `fan_out`
   distinct uniformly random columns (FixedProb with K = fan_out, include_self=True)."""
-  if device is None:
-    device = torch.device("cuda", torch.cuda.current_device())
   K = int(fan_out)
   if K < 0 or K > num_post:
     raise ValueError(f"fan_out {K} must lie in [0, num_post={num_post}]")
-  indices, indptr = _fixed_prob_device(int(num_pre), int(num_post), K, int(seed), False, True, None, device)
-  return indices.to(index_dtype), indptr.to(index_dtype)
+  gpu = _gpu_device(device)
+  indices, indptr = _fixed_prob_device(int(num_pre), int(num_post), K, int(seed), False, True, None, gpu)
+  target = gpu if device is None else torch.device(device)
+  return indices.to(index_dtype).to(target), indptr.to(index_dtype).to(target)
 
 
 class FixedProb:
@@ -108,7 +120,7 @@ class FixedProb:
     return self
 
   def _device(self):
-    return self.device if self.device is not None else torch.device("cuda", torch.cuda.current_device())
+    return _gpu_device(self.device)
 
   def build_csr(self):
     """(indices, indptr), int32, on the device."""
@@ -127,7 +139,8 @@ class FixedProb:
       if n_sel > 0:
         mask[torch.topk(keys, n_sel, largest=False).indices] = 1
     indices, indptr = _fixed_prob_device(m, n, K, self.seed, self.allow_multi_conn, self.include_self, mask, dev)
-    return indices, indptr.to(torch.int32)
+    target = dev if self.device is None else torch.device(self.device)
+    return indices.to(target), indptr.to(torch.int32).to(target)
 
   def build_coo(self):
     """(pre_ids, post_ids), int32."""

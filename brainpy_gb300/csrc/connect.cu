@@ -180,6 +180,17 @@ static bp_status fixed_prob_check(const char* who, int64_t m, int64_t n, int32_t
   return BP_OK;
 }
 
+// true when p is memory the device can write (device or managed): the generator is a setup
+// call, so it checks its output pointers instead of faulting on host addresses
+static bool device_writable(const void* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
 }  // namespace bp
 
 using namespace bp;
@@ -193,6 +204,8 @@ bp_status bp_fixed_prob_row_lengths(int64_t m, int64_t n, int32_t K, uint64_t se
   bp_status s = fixed_prob_check("fixed_prob_row_lengths", m, n, K, allow_multi, include_self);
   if (s != BP_OK || m == 0) return s;
   BP_REQUIRE(lengths != nullptr, BP_EINVAL, "fixed_prob_row_lengths: null lengths");
+  BP_REQUIRE(device_writable(lengths) && (!row_mask || device_writable(row_mask)), BP_EINVAL,
+             "fixed_prob_row_lengths: lengths and row_mask must be device memory");
   cudaStream_t st = as_cuda(stream);
   if (K == 0 || n == 0) {
     BP_CUDA_TRY(cudaMemsetAsync(lengths, 0, sizeof(int32_t) * (size_t)m, st));
@@ -208,6 +221,8 @@ bp_status bp_fixed_prob_fill(int64_t m, int64_t n, int32_t K, uint64_t seed, int
   bp_status s = fixed_prob_check("fixed_prob_fill", m, n, K, allow_multi, include_self);
   if (s != BP_OK || m == 0 || K == 0 || n == 0) return s;
   BP_REQUIRE(indptr && indices, BP_EINVAL, "fixed_prob_fill: null indptr/indices");
+  BP_REQUIRE(device_writable(indices) && device_writable(indptr) && (!row_mask || device_writable(row_mask)),
+             BP_EINVAL, "fixed_prob_fill: indptr, indices and row_mask must be device memory");
   ScopedKernelTimer tk(as_cuda(stream));
   return launch_fixed_prob<true>(m, n, K, seed, allow_multi, include_self ? 0 : 1, row_mask, indptr, indices,
                                  as_cuda(stream));

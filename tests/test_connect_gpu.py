@@ -68,3 +68,19 @@ def test_large_distinct_and_uniform(bplib):
   seg = torch.bincount((rows // 27840 + torch.arange(m, device=rows.device)[:, None] * 36).reshape(-1),
                        minlength=m * 36).view(m, 36)[:, :35].to(torch.float64)
   assert abs(float(seg.mean()) - 27.84) < 0.05 and 24.0 < float(seg.var()) < 30.0
+
+
+def test_host_device_arrays(bplib):
+  """Arrays wanted on the host are built on the GPU and copied; the C entry points refuse
+  host output pointers (checked before any launch)."""
+  import ctypes
+  from brainpy_gb300 import _lib
+  from brainpy_gb300.connect import fixed_prob_csr
+  ind_c, ptr_c = fixed_prob_csr(300, 500, 20, seed=3, device="cpu")
+  ind_g, ptr_g = fixed_prob_csr(300, 500, 20, seed=3)
+  assert ind_c.device.type == "cpu" and torch.equal(ind_c, ind_g.cpu()) and torch.equal(ptr_c, ptr_g.cpu())
+  host_ind = torch.empty(300 * 20, dtype=torch.int32)
+  host_ptr = torch.arange(301, dtype=torch.int64) * 20
+  st = _lib.lib().bp_fixed_prob_fill(300, 500, 20, 3, 0, 1, None, ctypes.c_void_p(host_ptr.data_ptr()),
+                                     ctypes.c_void_p(host_ind.data_ptr()), None)
+  assert st == _lib.BP_EINVAL

@@ -44,6 +44,8 @@ SIGNATURES = {
     "bp_fixed_prob_fill": (_c_i32, [_c_i64, _c_i64, _c_i32, ctypes.c_uint64, _c_i32, _c_i32, _c_ptr, _c_ptr, _c_ptr,
                                     _c_ptr]),
     "bp_stdp_workspace_size": (_c_size, [_c_i64]),
+    "bp_spike_ring_record": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_i32, _c_i64, _c_ptr, _c_ptr]),
+    "bp_spike_ring_read": (_c_i32, [_c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_i32, _c_i64, _c_ptr, _c_ptr, _c_ptr]),
     "bp_csr_on_pre_update": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_ptr, _c_i32,
                                       _c_ptr, _c_f32, _c_f32, _c_ptr, _c_size, _c_ptr]),
     "bp_csc_on_post_update": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_ptr,

@@ -250,6 +250,36 @@ __global__ void __launch_bounds__(kNetThreads, 1) net_cluster_kernel(const bp_ne
   cluster.sync();  // no CTA leaves while another may still read its lists
 }
 
+// Spike history of the per-operator path (the persistent runner keeps the same layout in shared
+// memory): ring[slot][w], bit b = neuron 32 w + b, step T in slot T mod L.  The time index is
+// step (+ *step_dev when given, for CUDA-graph replay).
+__global__ void __launch_bounds__(256) spike_ring_record_kernel(const uint8_t* __restrict__ spike, int64_t n,
+                                                                uint32_t* __restrict__ ring, int32_t L, int64_t words,
+                                                                int64_t step, const int32_t* __restrict__ step_dev) {
+  const int64_t T = step + (step_dev ? (int64_t)__ldg(step_dev) : 0);
+  uint32_t* row = ring + (int64_t)net_pos_mod(T, L) * words;
+  const int lane = threadIdx.x & 31;
+  for (int64_t k0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) & ~31ll; k0 < words * 32;
+       k0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = k0 + lane;
+    const uint32_t m = __ballot_sync(0xffffffffu, k < n && spike[k]);
+    if (lane == 0) row[k0 >> 5] = m;
+  }
+}
+
+// out[k] = bit of neuron lo + k in the slot of step T - delay (k < count)
+__global__ void __launch_bounds__(256) spike_ring_read_kernel(const uint32_t* __restrict__ ring, int32_t L,
+                                                              int64_t words, int64_t lo, int64_t count, int32_t delay,
+                                                              int64_t step, const int32_t* __restrict__ step_dev,
+                                                              uint8_t* __restrict__ out) {
+  const int64_t T = step + (step_dev ? (int64_t)__ldg(step_dev) : 0);
+  const uint32_t* row = ring + (int64_t)net_pos_mod(T - delay, L) * words;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t g = lo + k;
+    out[k] = (uint8_t)((__ldg(row + (g >> 5)) >> (g & 31)) & 1u);
+  }
+}
+
 }  // namespace bp
 
 using namespace bp;
@@ -287,6 +317,35 @@ bp_status bp_lif_coba_step_dev(const bp_lif_params* params, int64_t n, float* V,
   if (g > maxb) g = maxb;
   lif_step_kernel<<<(int)g, 256, 0, st>>>(*params, n, V, ge, gi, t_last, spike, dge, dgi, step_offset, step_dev, dt);
   return check_launch("lif_step_kernel");
+}
+
+bp_status bp_spike_ring_record(const uint8_t* spike, int64_t n, uint32_t* ring, int32_t ring_len, int64_t step,
+                               const int32_t* step_dev, bp_stream_t stream) {
+  clear_error();
+  BP_REQUIRE(n >= 0 && ring_len >= 1, BP_EINVAL, "spike_ring_record: n >= 0 and ring_len >= 1 required");
+  if (n == 0) return BP_OK;
+  BP_REQUIRE(spike && ring, BP_EINVAL, "spike_ring_record: null pointer");
+  const int64_t words = (n + 31) / 32;
+  int64_t g = (words * 32 + 255) / 256;
+  const int64_t maxb = (int64_t)device_sm_count() * 16;
+  if (g > maxb) g = maxb;
+  spike_ring_record_kernel<<<(int)g, 256, 0, as_cuda(stream)>>>(spike, n, ring, ring_len, words, step, step_dev);
+  return check_launch("spike_ring_record_kernel");
+}
+
+bp_status bp_spike_ring_read(const uint32_t* ring, int32_t ring_len, int64_t n, int64_t lo, int64_t count,
+                             int32_t delay, int64_t step, const int32_t* step_dev, uint8_t* out, bp_stream_t stream) {
+  clear_error();
+  BP_REQUIRE(ring_len >= 1 && n >= 0 && lo >= 0 && count >= 0 && lo + count <= n, BP_EINVAL,
+             "spike_ring_read: bad range [%lld, %lld) of %lld", (long long)lo, (long long)(lo + count), (long long)n);
+  if (count == 0) return BP_OK;
+  BP_REQUIRE(ring && out, BP_EINVAL, "spike_ring_read: null pointer");
+  int64_t g = (count + 255) / 256;
+  const int64_t maxb = (int64_t)device_sm_count() * 16;
+  if (g > maxb) g = maxb;
+  spike_ring_read_kernel<<<(int)g, 256, 0, as_cuda(stream)>>>(ring, ring_len, (n + 31) / 32, lo, count, delay, step,
+                                                               step_dev, out);
+  return check_launch("spike_ring_read_kernel");
 }
 
 int32_t bp_net_max_tiles(void) { return kNetMaxTiles; }

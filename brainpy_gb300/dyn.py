@@ -35,29 +35,11 @@ def delay_steps(delay, dt):
   return 0 if delay is None else int(math.ceil(float(delay) / float(dt)))
 
 
-_BIT_SHIFTS = {}
+class _DevStep:
+  """A device-side time index: *step_dev + offset (CUDA-graph replay)."""
 
-
-def _shifts(dev):
-  t = _BIT_SHIFTS.get(dev)
-  if t is None:
-    t = torch.arange(32, dtype=torch.int64, device=dev)
-    _BIT_SHIFTS[dev] = t
-  return t
-
-
-def _pack_bits(spike, words):
-  """bool [n] -> int32 [words], bit b of word w = spike[32 w + b]."""
-  b = torch.zeros(words * 32, dtype=torch.int64, device=spike.device)
-  b[: spike.shape[0]] = spike.to(torch.int64)
-  v = (b.view(words, 32) << _shifts(spike.device)).sum(dim=1)
-  return torch.where(v >= (1 << 31), v - (1 << 32), v).to(torch.int32)
-
-
-def _unpack_bits(words_row, n):
-  """int32 [words] -> bool [n]."""
-  v = words_row.to(torch.int64) & 0xFFFFFFFF
-  return ((v.unsqueeze(-1) >> _shifts(words_row.device)) & 1).reshape(-1)[:n].to(torch.bool)
+  def __init__(self, step_dev, offset):
+    self.step_dev, self.offset = step_dev, int(offset)
 
 
 @dataclass
@@ -233,29 +215,33 @@ class EINetwork:
   def _delayed_spikes(self, T):
     """(excitatory, inhibitory) spike vectors the projections of step T read: self.spike
     when the group has no delay, otherwise the history slot of step T - d.  T is an int or a
-    one-element device tensor (CUDA-graph replay)."""
+    _DevStep (CUDA-graph replay)."""
     ne = self.n_exc
+    if not hasattr(self, "_dspk"):
+      self._dspk = torch.zeros(self.n, dtype=torch.bool, device=self.device)
+    step, sdev = (T.offset, T.step_dev) if isinstance(T, _DevStep) else (int(T), None)
     out = []
-    for d, sl in ((self.d_e, slice(0, ne)), (self.d_i, slice(ne, self.n))):
+    for d, lo, hi in ((self.d_e, 0, ne), (self.d_i, ne, self.n)):
       if d == 0:
-        out.append(self.spike[sl])
+        out.append(self.spike[lo:hi])
         continue
-      if isinstance(T, torch.Tensor):
-        row = self.ring.index_select(0, torch.remainder(T.to(torch.int64) - d, self.ring_len))[0]
-      else:
-        row = self.ring[(T - d) % self.ring_len]
-      out.append(_unpack_bits(row, self.n)[sl])
+      dst = self._dspk[lo:hi]
+      st = _lib.lib().bp_spike_ring_read(_lib.ptr(self.ring), self.ring_len, self.n, lo, hi - lo, d, step,
+                                         _lib.ptr(sdev) if sdev is not None else None,
+                                         _lib.ptr(dst.view(torch.uint8)), _lib.stream_handle(self.device))
+      _lib.check(st, "spike_ring_read")
+      out.append(dst)
     return out
 
   def _record_spikes(self, T):
     """Stores self.spike as step T's history slot."""
     if self.ring is None:
       return
-    packed = _pack_bits(self.spike, self.words)
-    if isinstance(T, torch.Tensor):
-      self.ring.index_copy_(0, torch.remainder(T.to(torch.int64), self.ring_len), packed.unsqueeze(0))
-    else:
-      self.ring[T % self.ring_len] = packed
+    step, sdev = (T.offset, T.step_dev) if isinstance(T, _DevStep) else (int(T), None)
+    st = _lib.lib().bp_spike_ring_record(_lib.ptr(self.spike.view(torch.uint8)), self.n, _lib.ptr(self.ring),
+                                         self.ring_len, step, _lib.ptr(sdev) if sdev is not None else None,
+                                         _lib.stream_handle(self.device))
+    _lib.check(st, "spike_ring_record")
 
   def _propagate_ops(self, T=None):
     """Conductance increments of one step (per-operator path): the rows' spikes of the
@@ -284,7 +270,7 @@ class EINetwork:
 
   def step_ops(self, dt, step_dev=None, offset=0):
     """One step through the per-operator path (propagation calls + neuron kernel)."""
-    T = self.t_step if step_dev is None else step_dev + offset
+    T = self.t_step if step_dev is None else _DevStep(step_dev, offset)
     dge, dgi = self._propagate_ops(T)
     if step_dev is None:
       lif_coba_step(self.params, self.V, self.ge, self.gi, self.t_last, self.spike, dge, dgi, self.t_step, dt)

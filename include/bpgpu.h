@@ -330,6 +330,15 @@ typedef struct {
   uint32_t* ring;
 } bp_net_desc;
 
+/* The spike history of bp_net_desc for the per-operator path: bp_spike_ring_record stores the
+ * n spikes (bytes) of step T as bits in slot T mod ring_len; bp_spike_ring_read writes, for
+ * neurons [lo, lo + count), the bits of step T - delay as bytes into out.  T = step, plus
+ * *step_dev when step_dev is not NULL (device-side time index for CUDA-graph replay). */
+bp_status bp_spike_ring_record(const uint8_t* spike, int64_t n, uint32_t* ring, int32_t ring_len, int64_t step,
+                               const int32_t* step_dev, bp_stream_t stream);
+bp_status bp_spike_ring_read(const uint32_t* ring, int32_t ring_len, int64_t n, int64_t lo, int64_t count,
+                             int32_t delay, int64_t step, const int32_t* step_dev, uint8_t* out, bp_stream_t stream);
+
 /* largest n_tiles (cluster size) bp_net_run accepts, and the tile width it expects */
 int32_t bp_net_max_tiles(void);
 int32_t bp_net_tile_width(void);

@@ -211,6 +211,76 @@ __global__ void __launch_bounds__(256) ecsr_n_kernel(const IdxT* __restrict__ in
   }
 }
 
+// transpose=0 when the event vector fits shared memory as bits (n <= kEvBitsMax * 8): one CTA
+// per SM packs the events into bits once, then its warps stride over rows, each lane keeping 8
+// index loads in flight and testing the bits in shared memory -- no per-entry gather from L2.
+// Same arithmetic as ecsr_n_kernel (counts, or the lane's in-order sum of weights).
+constexpr size_t kEvBitsMax = 200 * 1024;
+constexpr int kNBitsUnroll = 8;
+
+template <typename IdxT, bool HOMO, int ET>
+__global__ void __launch_bounds__(1024, 1) ecsr_n_bits_kernel(const IdxT* __restrict__ indptr,
+                                                              const IdxT* __restrict__ indices,
+                                                              const float* __restrict__ data, int64_t nnz, int64_t m,
+                                                              int64_t n, const void* __restrict__ events,
+                                                              float* __restrict__ out) {
+  extern __shared__ uint32_t evb[];
+  const bool vec_ok = ((reinterpret_cast<uintptr_t>(events) & 15u) == 0);
+  const int64_t nw = (n + 31) / 32;
+  for (int64_t w = threadIdx.x; w < nw; w += blockDim.x) {
+    const int64_t base = w * 32;
+    evb[w] = load_event_mask16<ET>(events, base, n, vec_ok) |
+             (load_event_mask16<ET>(events, base + 16, n, vec_ok) << 16);
+  }
+  __syncthreads();
+  const int lane = lane_id();
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < m; row += nwarps) {
+    int64_t b, e;
+    row_bounds(indptr, row, nnz, b, e);
+    unsigned cnt = 0;
+    float acc = 0.0f;
+    for (int64_t j0 = b + lane; j0 < e; j0 += 32 * kNBitsUnroll) {
+      int64_t c[kNBitsUnroll];
+#pragma unroll
+      for (int u = 0; u < kNBitsUnroll; ++u) c[u] = j0 + 32 * u < e ? (int64_t)indices[j0 + 32 * u] : -1;
+#pragma unroll
+      for (int u = 0; u < kNBitsUnroll; ++u) {
+        const bool on = (uint64_t)c[u] < (uint64_t)n && ((evb[c[u] >> 5] >> (c[u] & 31)) & 1u);
+        if (HOMO) cnt += on;
+        else if (on) acc += data[j0 + 32 * u];
+      }
+    }
+    if (HOMO) {
+      cnt = warp_sum(cnt);
+      if (lane == 0) out[row] = (float)cnt * data[0];
+    } else {
+      acc = warp_sum(acc);
+      if (lane == 0) out[row] = acc;
+    }
+  }
+}
+
+template <typename IdxT, bool HOMO, int ET>
+static bp_status launch_n_bits(const IdxT* indptr, const IdxT* indices, const float* data, int64_t nnz, int64_t m,
+                               int64_t n, const void* events, float* out, cudaStream_t st) {
+  auto kfn = ecsr_n_bits_kernel<IdxT, HOMO, ET>;
+  static bool configured[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!configured[dev]) {
+    BP_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEvBitsMax));
+    configured[dev] = true;
+  }
+  const size_t smem = (size_t)((n + 31) / 32) * sizeof(uint32_t);
+  int64_t grid = (m + 31) / 32;
+  if (grid > device_sm_count()) grid = device_sm_count();
+  if (grid < 1) grid = 1;
+  kfn<<<(unsigned)grid, 1024, smem, st>>>(indptr, indices, data, nnz, m, n, events, out);
+  return check_launch("ecsr_n_bits_kernel");
+}
+
 static int grid_for(int64_t work_items, int per_block, int max_blocks) {
   int64_t g = (work_items + per_block - 1) / per_block;
   if (g < 1) g = 1;
@@ -276,8 +346,17 @@ template <typename IdxT, bool HOMO>
 static bp_status ecsr_n_dispatch(const float* data, const IdxT* indices, const IdxT* indptr, int64_t nnz,
                                  const void* events, bp_etype et, int64_t m, int64_t n, float* out,
                                  cudaStream_t st) {
-  const int grid = grid_for(m, 8, device_sm_count() * 16);
   ScopedKernelTimer tk(st);
+  if ((size_t)((n + 31) / 32) * sizeof(uint32_t) <= kEvBitsMax && m >= 4096) {
+    switch (et) {
+      case BP_EV_BOOL: return launch_n_bits<IdxT, HOMO, BP_EV_BOOL>(indptr, indices, data, nnz, m, n, events, out, st);
+      case BP_EV_F32_POS:
+        return launch_n_bits<IdxT, HOMO, BP_EV_F32_POS>(indptr, indices, data, nnz, m, n, events, out, st);
+      case BP_EV_F32_NZ:
+        return launch_n_bits<IdxT, HOMO, BP_EV_F32_NZ>(indptr, indices, data, nnz, m, n, events, out, st);
+    }
+  }
+  const int grid = grid_for(m, 8, device_sm_count() * 16);
   switch (et) {
     case BP_EV_BOOL:
       ecsr_n_kernel<IdxT, HOMO, BP_EV_BOOL><<<grid, 256, 0, st>>>(indptr, indices, data, nnz, m, n, events, out);

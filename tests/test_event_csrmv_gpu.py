@@ -250,3 +250,24 @@ def test_plan_autotune_and_every_variant(ev, orc):
   from brainpy_gb300 import _lib
   with pytest.raises(_lib.BPError):
     plan.csrmv(e, w)
+
+
+@pytest.mark.parametrize("n,evkind", [(200_000, "bool"), (1_000_000, "float"), (2_000_000, "bool")])
+def test_non_transpose_bits_path(ev, orc, n, evkind):
+  """transpose=0 with the event vector as bits in shared memory (n <= 1.6M), and beyond it
+  the per-entry gather kernel: counts bit-exact, weights within the FP32 bar."""
+  from brainpy_gb300.connect import fixed_prob_csr
+  m, k = 50_000, 300
+  ind, ptr = fixed_prob_csr(m, n, k, seed=12)
+  ind_h, ptr_h = ind.cpu().numpy(), ptr.cpu().numpy()
+  rng = np.random.default_rng(13)
+  mask = rng.random(n) < 0.05
+  events = mask if evkind == "bool" else (rng.normal(size=n) * mask).astype(np.float32)
+  e = torch.as_tensor(events, device="cuda")
+  y = ev.csrmv(0.25, ind, ptr, e, shape=(m, n), transpose=False).cpu().numpy()
+  r = orc.event_csrmv(np.float32(0.25), ind_h, ptr_h, events, (m, n), False)
+  np.testing.assert_array_equal(y, r["count32"])
+  heter = rng.normal(size=ind_h.size).astype(np.float32)
+  y = ev.csrmv(torch.as_tensor(heter, device="cuda"), ind, ptr, e, shape=(m, n), transpose=False).cpu().numpy()
+  r = orc.event_csrmv(heter, ind_h, ptr_h, events, (m, n), False)
+  assert scaled_err(y, r["out64"], r["abs64"]) < TOL

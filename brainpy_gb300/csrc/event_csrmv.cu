@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(256) ecsr_n_kernel(const IdxT* __restrict__ in
 // index loads in flight and testing the bits in shared memory -- no per-entry gather from L2.
 // Same arithmetic as ecsr_n_kernel (counts, or the lane's in-order sum of weights).
 constexpr size_t kEvBitsMax = 200 * 1024;
-constexpr int kNBitsUnroll = 8;
+constexpr int kNBitsUnroll = 16;
 
 template <typename IdxT, bool HOMO, int ET>
 __global__ void __launch_bounds__(1024, 1) ecsr_n_bits_kernel(const IdxT* __restrict__ indptr,

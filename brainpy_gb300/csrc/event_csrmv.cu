@@ -212,8 +212,9 @@ __global__ void __launch_bounds__(256) ecsr_n_kernel(const IdxT* __restrict__ in
 }
 
 // transpose=0 when the event vector fits shared memory as bits (n <= kEvBitsMax * 8): one CTA
-// per SM packs the events into bits once, then its warps stride over rows, each lane keeping 8
-// index loads in flight and testing the bits in shared memory -- no per-entry gather from L2.
+// per SM packs the events into bits once, then its warps stride over rows, each lane keeping
+// kNBitsUnroll index loads in flight and testing the bits in shared memory -- no per-entry
+// gather from L2.
 // Same arithmetic as ecsr_n_kernel (counts, or the lane's in-order sum of weights).
 constexpr size_t kEvBitsMax = 200 * 1024;
 constexpr int kNBitsUnroll = 16;

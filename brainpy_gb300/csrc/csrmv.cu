@@ -20,6 +20,8 @@ __device__ __forceinline__ void csr_row_bounds(const IdxT* indptr, int64_t row, 
   e = e < b ? b : (e > nnz ? nnz : e);
 }
 
+constexpr int kNUnroll = 8;
+
 template <typename IdxT, bool HOMO>
 __global__ void __launch_bounds__(256) csrmv_n_kernel(const IdxT* __restrict__ indptr, const IdxT* __restrict__ indices,
                                                       const float* __restrict__ data, int64_t nnz, int64_t m,
@@ -31,23 +33,18 @@ __global__ void __launch_bounds__(256) csrmv_n_kernel(const IdxT* __restrict__ i
     csr_row_bounds(indptr, row, nnz, b, e);
     float acc = 0.0f;
     int64_t j = b + lane;
-    for (; j + 96 < e; j += 128) {
-      int64_t c0 = (int64_t)indices[j], c1 = (int64_t)indices[j + 32];
-      int64_t c2 = (int64_t)indices[j + 64], c3 = (int64_t)indices[j + 96];
-      float x0 = (uint64_t)c0 < (uint64_t)n ? __ldg(x + c0) : 0.0f;
-      float x1 = (uint64_t)c1 < (uint64_t)n ? __ldg(x + c1) : 0.0f;
-      float x2 = (uint64_t)c2 < (uint64_t)n ? __ldg(x + c2) : 0.0f;
-      float x3 = (uint64_t)c3 < (uint64_t)n ? __ldg(x + c3) : 0.0f;
-      if (HOMO) {
-        acc += x0;
-        acc += x1;
-        acc += x2;
-        acc += x3;
-      } else {
-        acc = fmaf(data[j], x0, acc);
-        acc = fmaf(data[j + 32], x1, acc);
-        acc = fmaf(data[j + 64], x2, acc);
-        acc = fmaf(data[j + 96], x3, acc);
+    // kNUnroll entries per lane in flight (index loads, then the gathers), summed in j order
+    for (; j + 32 * (kNUnroll - 1) < e; j += 32 * kNUnroll) {
+      int64_t c[kNUnroll];
+      float xv[kNUnroll];
+#pragma unroll
+      for (int u = 0; u < kNUnroll; ++u) c[u] = (int64_t)indices[j + 32 * u];
+#pragma unroll
+      for (int u = 0; u < kNUnroll; ++u) xv[u] = (uint64_t)c[u] < (uint64_t)n ? __ldg(x + c[u]) : 0.0f;
+#pragma unroll
+      for (int u = 0; u < kNUnroll; ++u) {
+        if (HOMO) acc += xv[u];
+        else acc = fmaf(data[j + 32 * u], xv[u], acc);
       }
     }
     for (; j < e; j += 32) {

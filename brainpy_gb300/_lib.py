@@ -66,6 +66,8 @@ SIGNATURES = {
     "bp_event_csrmv_planned": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_i32, _c_ptr, _c_i32, _c_ptr, _c_size, _c_ptr]),
     "bp_csrmv_planned": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i32, _c_ptr, _c_size, _c_ptr]),
     "bp_event_csrmv_planned_batch_workspace_size": (_c_size, [_c_ptr, _c_i32]),
+    "bp_csrmv_planned_n_workspace_size": (_c_size, [_c_ptr]),
+    "bp_csrmv_planned_n": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_size, _c_ptr]),
     "bp_event_csrmv_planned_batch": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_i32, _c_i32, _c_ptr, _c_i32, _c_ptr, _c_size,
                                               _c_ptr]),
     "bp_csrmv_planned_batch": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_i32, _c_ptr, _c_i32, _c_ptr, _c_size, _c_ptr]),

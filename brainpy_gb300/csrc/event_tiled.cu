@@ -596,6 +596,63 @@ static bp_status compact_blocked(const void* events, bp_etype et, int64_t m, int
   return BP_EINVAL;
 }
 
+// ---------------------------------------------------------------------------
+// sparse.csrmv, transpose=0, on a plan: y[i] = sum_j A[i, j] x[j].  CTA (tile t, row split s)
+// stages x[t * tile_w, (t + 1) * tile_w) in shared memory and walks row i's segment for tile t
+// (thread per row): the dense-vector gathers come from shared memory instead of L2.  Partial
+// sums go to part[t][m] (coalesced); csrmv_n_reduce_kernel adds them in tile order.
+// ---------------------------------------------------------------------------
+template <bool HETER>
+__global__ void __launch_bounds__(1024) csrmv_n_planned_kernel(const uint32_t* __restrict__ seg_off,
+                                                               const uint16_t* __restrict__ idx,
+                                                               const float* __restrict__ w, const float* __restrict__ x,
+                                                               int64_t m, int64_t n, int32_t tile_w, int32_t n_tiles,
+                                                               int32_t splits, float* __restrict__ part) {
+  extern __shared__ float xs[];
+  const int t = blockIdx.x % n_tiles;
+  const int sp = blockIdx.x / n_tiles;
+  const int64_t col0 = (int64_t)t * tile_w;
+  for (int k = threadIdx.x; k < tile_w; k += blockDim.x) xs[k] = col0 + k < n ? __ldg(x + col0 + k) : 0.0f;
+  __syncthreads();
+  const int64_t r0 = (int64_t)sp * m / splits, r1 = (int64_t)(sp + 1) * m / splits;
+  const int64_t so_stride = (int64_t)n_tiles + 1;
+  const uint32_t lim = (uint32_t)tile_w;
+  for (int64_t row = r0 + threadIdx.x; row < r1; row += blockDim.x) {
+    const uint32_t* so = seg_off + row * so_stride + t;
+    const uint32_t st = __ldg(so), en = __ldg(so + 1);
+    float acc = 0.0f;
+    for (uint32_t c = st; c < en; ++c) {
+      const uint4 v = __ldg(reinterpret_cast<const uint4*>(idx + 8ull * c));
+      const uint32_t q[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
+                             v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
+      if (HETER) {
+        const float4 w0 = __ldg(reinterpret_cast<const float4*>(w + 8ull * c));
+        const float4 w1 = __ldg(reinterpret_cast<const float4*>(w + 8ull * c + 4));
+        const float ww[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          if (q[k] < lim) acc = fmaf(ww[k], xs[q[k]], acc);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k)
+          if (q[k] < lim) acc += xs[q[k]];
+      }
+    }
+    part[(int64_t)t * m + row] = acc;
+  }
+}
+
+__global__ void __launch_bounds__(256) csrmv_n_reduce_kernel(const float* __restrict__ part, int64_t m,
+                                                             int32_t n_tiles, const float* __restrict__ w_homo,
+                                                             float* __restrict__ out) {
+  const float w = w_homo ? __ldg(w_homo) : 1.0f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.0f;
+    for (int t = 0; t < n_tiles; ++t) s += __ldg(part + (int64_t)t * m + i);
+    out[i] = w_homo ? __fmul_rn(s, w) : s;
+  }
+}
+
 // how many clusters of R CTAs with `smem` bytes of shared memory can be resident at once
 static int max_active_clusters(int R, size_t smem) {
   auto kfn = ecsr_t_tiled_kernel<kCount, 4, 1, true, false>;
@@ -840,6 +897,70 @@ bp_status bp_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, const f
   clear_error();
   return planned_batch("csrmv_planned", plan, w_homo, vec, BP_EV_F32_NZ, true, 1, out, cluster, workspace,
                        workspace_bytes, as_cuda(stream));
+}
+
+size_t bp_csrmv_planned_n_workspace_size(const bp_csr_plan* plan) {
+  if (!plan || plan->m <= 0 || plan->n_tiles <= 0) return 256;
+  return align_up(sizeof(float) * (size_t)plan->m * (size_t)plan->n_tiles, 256);
+}
+
+bp_status bp_csrmv_planned_n(const bp_csr_plan* plan, const float* w_homo, const float* vec, float* out,
+                             void* workspace, size_t workspace_bytes, bp_stream_t stream) {
+  clear_error();
+  cudaStream_t st = as_cuda(stream);
+  BP_REQUIRE(plan != nullptr && plan->mem != nullptr, BP_EINVAL, "csrmv_planned_n: null plan");
+  const int64_t m = plan->m, n = plan->n;
+  if (m == 0) return BP_OK;
+  BP_REQUIRE(out != nullptr, BP_EINVAL, "csrmv_planned_n: null out");
+  if (n == 0 || plan->nnz == 0) {
+    BP_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * (size_t)m, st));
+    return BP_OK;
+  }
+  BP_REQUIRE(vec != nullptr, BP_EINVAL, "csrmv_planned_n: null vector");
+  const bool homo = plan->heter == 0;
+  BP_REQUIRE(!homo || w_homo != nullptr, BP_EINVAL, "csrmv_planned_n: homogeneous plan needs w_homo");
+  const size_t need = bp_csrmv_planned_n_workspace_size(plan);
+  BP_REQUIRE(workspace && workspace_bytes >= need, BP_ENOMEM, "csrmv_planned_n: workspace %zu < %zu", workspace_bytes,
+             need);
+  const size_t smem = sizeof(float) * (size_t)plan->tile_w;
+  BP_REQUIRE(smem <= (size_t)max_smem_optin() - kStaticSmemReserve, BP_ENOTSUP,
+             "csrmv_planned_n: tile of %d columns does not fit shared memory", plan->tile_w);
+  PlanView v = plan_view(plan);
+  // row splits: enough CTAs for two per SM
+  const int nt = plan->n_tiles;
+  int splits = (int)((2 * device_sm_count() + nt - 1) / nt);
+  if (splits < 1) splits = 1;
+  if ((int64_t)splits > m) splits = (int)m;
+  float* part = static_cast<float*>(workspace);
+  static bool configured[2][64] = {{false}};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  ScopedKernelTimer tk(st);
+  if (homo) {
+    if (!configured[0][dev]) {
+      BP_CUDA_TRY(cudaFuncSetAttribute(csrmv_n_planned_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       max_smem_optin() - (int)kStaticSmemReserve));
+      configured[0][dev] = true;
+    }
+    csrmv_n_planned_kernel<false><<<nt * splits, 1024, smem, st>>>(v.seg_off, v.idx, nullptr, vec, m, n,
+                                                                   plan->tile_w, nt, splits, part);
+  } else {
+    if (!configured[1][dev]) {
+      BP_CUDA_TRY(cudaFuncSetAttribute(csrmv_n_planned_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       max_smem_optin() - (int)kStaticSmemReserve));
+      configured[1][dev] = true;
+    }
+    csrmv_n_planned_kernel<true><<<nt * splits, 1024, smem, st>>>(v.seg_off, v.idx, v.w, vec, m, n, plan->tile_w, nt,
+                                                                  splits, part);
+  }
+  bp_status s = check_launch("csrmv_n_planned_kernel");
+  if (s != BP_OK) return s;
+  int64_t g = (m + 255) / 256;
+  const int64_t maxb = (int64_t)device_sm_count() * 16;
+  if (g > maxb) g = maxb;
+  csrmv_n_reduce_kernel<<<(unsigned)g, 256, 0, st>>>(part, m, nt, homo ? w_homo : nullptr, out);
+  return check_launch("csrmv_n_reduce_kernel");
 }
 
 bp_status bp_csrmv_planned_batch(const bp_csr_plan* plan, const float* w_homo, const float* vec, int32_t batch,

@@ -166,6 +166,29 @@ class CSRPlan:
       _lib.check(st, "csrmv_planned_batch")
     return out
 
+  def sparse_n(self, vector, data=None, out=None):
+    """out (m) = A vector on this plan (sparse.csrmv, transpose=False): column tiles of the
+    vector staged in shared memory, per-tile partial row sums added in tile order."""
+    m, n = self.shape
+    if vector.shape[0] != n:
+      raise ValueError(f"Shape mismatch, mat {self.shape} @ vec ({vector.shape[0]},).")
+    if out is None:
+      out = torch.empty(m, dtype=torch.float32, device=self.device)
+    w = 0
+    if not self.heter:
+      w = (data if data is not None else self._one).data_ptr()
+    sp = _lib.raw_stream(self.device)
+    need = self._L.bp_csrmv_planned_n_workspace_size(self._cref)
+    key = ("n", sp)
+    ws = self._ws.get(key)
+    if ws is None or ws.numel() < need:
+      ws = torch.empty(max(need, 1), dtype=torch.uint8, device=self.device)
+      self._ws[key] = ws
+    st = self._L.bp_csrmv_planned_n(self._cref, w, vector.data_ptr(), out.data_ptr(), ws.data_ptr(), ws.numel(), sp)
+    if st:
+      _lib.check(st, "csrmv_planned_n")
+    return out
+
   def sparse_t(self, vector, data=None, out=None):
     """out (n) = A^T vector on this plan (sparse.csrmv, transpose=True)."""
     dev = self.device

@@ -42,10 +42,12 @@ def _csrmv(data, indices, indptr, vector, shape, transpose, out=None, use_plan=T
   itype = index_type(indices, "indices")
   if index_type(indptr, "indptr") != itype:
     raise ValueError("indices and indptr must have the same integer type.")
-  if transpose and use_plan:
+  if use_plan:
     plan = _event._cached_plan(data, indices, indptr, (m, n))
     if plan is not None:
-      return plan.sparse_t(vector, None if plan.heter else data, out=out)
+      if transpose:
+        return plan.sparse_t(vector, None if plan.heter else data, out=out)
+      return plan.sparse_n(vector, None if plan.heter else data, out=out)
   n_out = n if transpose else m
   if out is None:
     out = torch.empty(n_out, dtype=torch.float32, device=dev)

@@ -235,6 +235,16 @@ bp_status bp_event_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, c
 bp_status bp_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, const float* vec, float* out,
                            int32_t cluster, void* workspace, size_t workspace_bytes, bp_stream_t stream);
 
+/* sparse.csrmv, transpose=0, on a plan: out (m) = A vec (vec length n).  Each CTA stages one
+ * column tile of vec in shared memory and sums its rows' segments for that tile; the per-tile
+ * partial sums (workspace: bp_csrmv_planned_n_workspace_size(plan) = 4 * m * n_tiles bytes)
+ * are added in tile order.  Homogeneous: w * (sum of the vector entries), as the reference's
+ * homogeneous non-transpose kernels apply the weight once (brainpy/_src/math/sparse/
+ * _csr_mv_taichi.py:53-65). */
+size_t bp_csrmv_planned_n_workspace_size(const bp_csr_plan* plan);
+bp_status bp_csrmv_planned_n(const bp_csr_plan* plan, const float* w_homo, const float* vec, float* out,
+                             void* workspace, size_t workspace_bytes, bp_stream_t stream);
+
 /* A batch of `batch` vectors (0..65535) through one plan in one launch pair -- the batched form
  * that replaces the reference's batching rule for these primitives, a sequential lax.scan of
  * single calls (brainpy/_src/math/op_register/utils.py:16-38, registered for event.csrmv at

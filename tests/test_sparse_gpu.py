@@ -89,3 +89,33 @@ def test_utils(sp):
   with pytest.raises(ValueError, match="Only support methods"):
     sp.csrmv(1.0, torch.as_tensor(ind, device="cuda"), torch.as_tensor(ptr, device="cuda"),
              torch.ones(n, device="cuda"), shape=(m, n), method="magic")
+
+
+@pytest.mark.parametrize("tile_w", [512, None])
+def test_planned_non_transpose_against_oracle(bplib, orc, tile_w):
+  """sparse.csrmv transpose=0 on a plan (column tiles of the vector in shared memory, per-tile
+  partial sums added in tile order), homogeneous and heterogeneous, against the FP64 oracle;
+  the public call takes the same path through the plan cache."""
+  from brainpy_gb300.connect import fixed_prob_csr
+  from brainpy_gb300.math import event, sparse
+  m, n, k = 3000, 50001, 400
+  ind, ptr = fixed_prob_csr(m, n, k, seed=9)
+  ind_h, ptr_h = ind.cpu().numpy(), ptr.cpu().numpy()
+  rng = np.random.default_rng(10)
+  x = (rng.normal(size=n) * (rng.random(n) < 0.7)).astype(np.float32)
+  heter = rng.normal(size=ind_h.size).astype(np.float32)
+  xd = torch.as_tensor(x, device="cuda")
+  ph = event.prepare(ind, ptr, shape=(m, n), tile_w=tile_w)
+  pw = event.prepare(ind, ptr, shape=(m, n), data=torch.as_tensor(heter, device="cuda"), tile_w=tile_w)
+  y = ph.sparse_n(xd, torch.tensor([-1.5], device="cuda")).cpu().numpy()
+  r = orc.csrmv(np.float32(-1.5), ind_h, ptr_h, x, (m, n), False)
+  assert scaled_err(y, r["out64"], r["abs64"]) < TOL
+  y = pw.sparse_n(xd).cpu().numpy()
+  r = orc.csrmv(heter, ind_h, ptr_h, x, (m, n), False)
+  assert scaled_err(y, r["out64"], r["abs64"]) < TOL
+  m2, n2 = 40000, 40000
+  ind2, ptr2 = fixed_prob_csr(m2, n2, 60, seed=2)
+  x2 = torch.randn(n2, device="cuda")
+  y2 = sparse.csrmv(0.5, ind2, ptr2, x2, shape=(m2, n2), transpose=False).cpu().numpy()
+  r = orc.csrmv(np.float32(0.5), ind2.cpu().numpy(), ptr2.cpu().numpy(), x2.cpu().numpy(), (m2, n2), False)
+  assert scaled_err(y2, r["out64"], r["abs64"]) < TOL

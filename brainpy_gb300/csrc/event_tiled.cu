@@ -599,8 +599,9 @@ static bp_status compact_blocked(const void* events, bp_etype et, int64_t m, int
 // ---------------------------------------------------------------------------
 // sparse.csrmv, transpose=0, on a plan: y[i] = sum_j A[i, j] x[j].  CTA (tile t, row split s)
 // stages x[t * tile_w, (t + 1) * tile_w) in shared memory and walks row i's segment for tile t
-// (thread per row): the dense-vector gathers come from shared memory instead of L2.  Partial
-// sums go to part[t][m] (coalesced); csrmv_n_reduce_kernel adds them in tile order.
+// (4 lanes per row, chunks c, c + 4, ...): the dense-vector gathers come from shared memory
+// instead of L2.  Partial sums go to part[t][m] (coalesced); csrmv_n_reduce_kernel adds them
+// in tile order.
 // ---------------------------------------------------------------------------
 template <bool HETER>
 __global__ void __launch_bounds__(1024) csrmv_n_planned_kernel(const uint32_t* __restrict__ seg_off,
@@ -617,11 +618,19 @@ __global__ void __launch_bounds__(1024) csrmv_n_planned_kernel(const uint32_t* _
   const int64_t r0 = (int64_t)sp * m / splits, r1 = (int64_t)(sp + 1) * m / splits;
   const int64_t so_stride = (int64_t)n_tiles + 1;
   const uint32_t lim = (uint32_t)tile_w;
-  for (int64_t row = r0 + threadIdx.x; row < r1; row += blockDim.x) {
-    const uint32_t* so = seg_off + row * so_stride + t;
-    const uint32_t st = __ldg(so), en = __ldg(so + 1);
+  // groups of 4 lanes per row: a segment's chunks are read as one contiguous run
+  const int gl = threadIdx.x & 3;
+  const int64_t groups = blockDim.x >> 2;
+  for (int64_t rb = r0; rb < r1; rb += groups) {
+    const int64_t row = rb + (threadIdx.x >> 2);
+    uint32_t st = 0, en = 0;
+    if (row < r1) {
+      const uint32_t* so = seg_off + row * so_stride + t;
+      st = __ldg(so);
+      en = __ldg(so + 1);
+    }
     float acc = 0.0f;
-    for (uint32_t c = st; c < en; ++c) {
+    for (uint32_t c = st + gl; c < en; c += 4) {
       const uint4 v = __ldg(reinterpret_cast<const uint4*>(idx + 8ull * c));
       const uint32_t q[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
                              v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
@@ -638,7 +647,9 @@ __global__ void __launch_bounds__(1024) csrmv_n_planned_kernel(const uint32_t* _
           if (q[k] < lim) acc += xs[q[k]];
       }
     }
-    part[(int64_t)t * m + row] = acc;
+    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+    if (gl == 0 && row < r1) part[(int64_t)t * m + row] = acc;
   }
 }
 

@@ -618,17 +618,24 @@ __global__ void __launch_bounds__(1024) csrmv_n_planned_kernel(const uint32_t* _
   const int64_t r0 = (int64_t)sp * m / splits, r1 = (int64_t)(sp + 1) * m / splits;
   const int64_t so_stride = (int64_t)n_tiles + 1;
   const uint32_t lim = (uint32_t)tile_w;
-  // groups of 4 lanes per row: a segment's chunks are read as one contiguous run
+  // groups of 4 lanes per row: a segment's chunks are read as one contiguous run; the next
+  // row's segment bounds load while the current row is summed
   const int gl = threadIdx.x & 3;
   const int64_t groups = blockDim.x >> 2;
-  for (int64_t rb = r0; rb < r1; rb += groups) {
-    const int64_t row = rb + (threadIdx.x >> 2);
-    uint32_t st = 0, en = 0;
+  auto bounds = [&](int64_t row, uint32_t& st, uint32_t& en) {
+    st = en = 0;
     if (row < r1) {
       const uint32_t* so = seg_off + row * so_stride + t;
       st = __ldg(so);
       en = __ldg(so + 1);
     }
+  };
+  uint32_t nst, nen;
+  bounds(r0 + (threadIdx.x >> 2), nst, nen);
+  for (int64_t rb = r0; rb < r1; rb += groups) {
+    const int64_t row = rb + (threadIdx.x >> 2);
+    const uint32_t st = nst, en = nen;
+    bounds(row + groups, nst, nen);
     float acc = 0.0f;
     for (uint32_t c = st + gl; c < en; c += 4) {
       const uint4 v = __ldg(reinterpret_cast<const uint4*>(idx + 8ull * c));

@@ -154,6 +154,14 @@ __global__ void __launch_bounds__(256) compact_blocked_kernel(const void* __rest
 //   kWRow   heterogeneous weights, dense vector x: float32 sum of w_ij * x_i
 enum { kCount = 0, kWeight = 1, kRowVal = 2, kWRow = 3 };
 
+// Threads of a tiled CTA: 1024 (64 registers a thread), except the per-synapse-weight modes
+// with two chunk rounds, whose double-buffered 48-byte chunks need more than 64 registers:
+// 768 threads (80 registers) there.
+template <int MODE, int RND>
+constexpr int tiled_threads() {
+  return ((MODE == kWeight || MODE == kWRow) && RND >= 2) ? 768 : kTiledThreads;
+}
+
 // Shared-memory reductions issued under a predicate (no branch): entries with index >= lim
 // are skipped -- the 0xFFFF padding, and every entry of a chunk given lim = 0.
 __device__ __forceinline__ void red_if(uint32_t x, uint32_t lim, uint32_t addr, uint32_t v) {
@@ -213,7 +221,7 @@ struct TiledArgs {
 // tile-local indices per chunk) and UB segments per group are loaded back to back before any
 // shared-memory atomic is issued.
 template <int MODE, int G, int RND, bool PF, bool BATCH>
-__global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const TiledArgs a) {
+__global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_kernel(const TiledArgs a) {
   constexpr bool HAS_W = (MODE == kWeight || MODE == kWRow);
   constexpr bool HAS_X = (MODE == kRowVal || MODE == kWRow);
   constexpr unsigned FULL = 0xffffffffu;
@@ -247,8 +255,9 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_tiled_kernel(const Ti
   // the compaction kernel of this call may still be running (programmatic dependent launch)
   cudaGridDependencySynchronize();
 
-  for (int g0 = b0; g0 < b1; g0 += kBlockGroup) {
-    const int ng = min(kBlockGroup, b1 - g0);
+  // groups of at most one compaction block per thread (nthr <= kBlockGroup)
+  for (int g0 = b0; g0 < b1; g0 += nthr) {
+    const int ng = min(nthr, b1 - g0);
     __syncthreads();  // s_boff of the previous group is no longer read
     int v = tid < ng ? counts[g0 + tid] : 0;
     int incl = v;
@@ -510,7 +519,7 @@ static bp_status launch_tiled_g(const TiledArgs& a, int R, cudaStream_t st) {
   BP_CUDA_TRY(prepare_kernel(kfn, done));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(a.n_tiles * R), (unsigned)a.batch, 1);
-  cfg.blockDim = dim3(kTiledThreads, 1, 1);
+  cfg.blockDim = dim3(tiled_threads<MODE, RND>(), 1, 1);
   cfg.dynamicSmemBytes = tiled_smem_bytes(a.acc_words);
   cfg.stream = st;
   cudaLaunchAttribute attr[2];
@@ -529,13 +538,16 @@ static bp_status launch_tiled_g(const TiledArgs& a, int R, cudaStream_t st) {
 // (lanes per segment, chunk rounds, L2 prefetch): the plan's chosen variant when set
 // (bp_csr_plan.variant = G | RND << 8 | PF << 16, e.g. from an autotuning pass), otherwise
 // from the mean segment length in 16-byte chunks; BPGPU_TILED=G,RND,PF overrides both.
-static void tiled_config(double chunks, int32_t variant, int& G, int& RND, int& PF) {
+static void tiled_config(double chunks, bool has_w, int32_t variant, int& G, int& RND, int& PF) {
   // measured on FixedProb rows (uniform columns) at N = 1e6, K = 1000 (3.9 chunks a segment,
-  // lengths spread as a multinomial): G=2, RND=2 31.6 us, flat distribution 33.0, G=4, RND=2
-  // 33.3, G=4, RND=1 37.1, G=8 38.0 at 2 % events
+  // lengths spread as a multinomial), back-to-back calls:
+  //   counts (homogeneous weight): G=2, RND=2 30.7 us at 2 % events, 100.0 at 10 %; G=4, RND=1
+  //     34.6 / 127.9; flat distribution 33.0 and G=8 38.0 at 2 %;
+  //   per-synapse weights (48 bytes a chunk): G=4, RND=1 58.9 / 237.7; G=8, RND=1 61.5 / 252.8;
+  //     G=2, RND=1 64.4 / 269.6; G=2, RND=2 (768 threads) 65.8 / 260.7.
   if (chunks <= 1.25) { G = 1; RND = 1; }
   else if (chunks <= 2.5) { G = 2; RND = 1; }
-  else if (chunks <= 5.0) { G = 2; RND = 2; }
+  else if (chunks <= 5.0) { G = has_w ? 4 : 2; RND = has_w ? 1 : 2; }
   else if (chunks <= 9.0) { G = 8; RND = 1; }
   else { G = 8; RND = 2; }
   PF = 0;  // measured: L2 prefetch of the next slice does not pay at 2-10 % event rates
@@ -560,7 +572,7 @@ static void tiled_config(double chunks, int32_t variant, int& G, int& RND, int& 
 template <int MODE>
 static bp_status launch_tiled(const TiledArgs& a, int R, double chunks, cudaStream_t st) {
   int G, RND, PF;
-  tiled_config(chunks, a.variant, G, RND, PF);
+  tiled_config(chunks, MODE == kWeight || MODE == kWRow, a.variant, G, RND, PF);
 #define BP_TILED_CASE(g, r)                                                                           \
   if (G == g && RND == r) {                                                                           \
     if (a.batch > 1) return launch_tiled_g<MODE, g, r, false, true>(a, R, st);                        \

@@ -138,6 +138,16 @@ def make_workload(args, device, n_vec=8):
   return data, ind, ptr, spikes
 
 
+def same_result(a, b, heter):
+  """Two results of the same call agree: bit for bit with a homogeneous weight (integer
+  counts x w); with per-synapse weights the float32 shared-memory sums are added in a
+  run-dependent order, so within 1e-5 of the largest magnitude."""
+  if not heter:
+    return torch.equal(a, b)
+  b = b.to(a.device)
+  return bool(((a - b).abs() <= 1e-5 * b.abs().max().clamp_min(1e-30)).all())
+
+
 def alg_bytes(n, active, k, heter):
   """Algorithmic bytes of one event.csrmv transpose call on the reference's CSR format:
   spikes (1 B/row) + indptr pair per active row + int32 index per event
@@ -263,7 +273,7 @@ def main():
   events_done = sum(active[i % nv] for i in range(args.steps)) * k
   # the graphed results equal eager calls on the same spikes
   for i in range(min(nv, args.steps)):
-    assert torch.equal(outs[i], step(i)), "graph replay and eager call disagree"
+    assert same_result(outs[i], step(i), args.weights == "heter"), "graph replay and eager call disagree"
   # replicas: the slowest rank's time, the events of all ranks
   from brainpy_gb300 import replicas
   step_ms, events_done = replicas.combine(step_ms, events_done)
@@ -340,7 +350,8 @@ def main():
   e2e_events = sum(active[i % nv] for i in range(args.steps)) * k
   torch.cuda.synchronize()
   for j in range(min(nv, args.steps)):  # the results read back are the device results
-    assert torch.equal(out_host[j], outs[j].cpu()), "e2e result differs from the device result"
+    assert same_result(out_host[j], outs[j].cpu(), args.weights == "heter"), \
+        "e2e result differs from the device result"
   e2e_ms, e2e_events = replicas.combine(e2e_ms, e2e_events)
   e2e = {"value": e2e_events / (e2e_ms * 1e-3), "unit": UNIT,
          "h2d_bytes_per_step": n + (4 if args.weights == "homo" else 0), "d2h_bytes_per_step": 4 * n}

@@ -192,8 +192,8 @@ __device__ __forceinline__ void accumulate8(uint32_t acc_s, uint4 v, float4 w0, 
 
 __device__ __forceinline__ uint4 ld_stream_u4(const uint16_t* p) { return __ldcs(reinterpret_cast<const uint4*>(p)); }
 __device__ __forceinline__ float4 ld_stream_f4(const float* p) { return __ldcs(reinterpret_cast<const float4*>(p)); }
-__device__ __forceinline__ void prefetch_l2(const void* p) {
-  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
 
 struct TiledArgs {
@@ -215,11 +215,11 @@ struct TiledArgs {
 // Warp-independent processing: after one CTA-wide prefix over this rank's compaction blocks,
 // every warp walks "slices" of 32 active rows (slices warp, warp + W, ...).  Lane l of a slice
 // owns row 32k + l and loads that row's segment bounds for this CTA's tile.  Pipeline per
-// warp: the row ids of slice k + 3W and the segment bounds of slice k + 2W are loaded, the
-// segments of slice k + W are prefetched into L2 (PF), and slice k is processed: groups of G
-// lanes take one segment each (lane gl loads 16-byte chunks gl, gl + G, ... -- RND rounds, 8
-// tile-local indices per chunk) and UB segments per group are loaded back to back before any
-// shared-memory atomic is issued.
+// warp: the row ids of slice k + 3W and the segment bounds of slice k + 2W are loaded, and
+// slice k is processed: groups of G lanes take one segment each (lane gl loads 16-byte chunks
+// gl, gl + G, ... -- RND rounds, 8 tile-local indices per chunk) and UB segments per group are
+// loaded back to back before any shared-memory atomic is issued.  With PF, a lane whose
+// segment is longer than RND * G chunks also prefetches its next chunk into L1 with the unit.
 template <int MODE, int G, int RND, bool PF, bool BATCH>
 __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_kernel(const TiledArgs a) {
   constexpr bool HAS_W = (MODE == kWeight || MODE == kWRow);
@@ -356,6 +356,16 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
             U.w1[u][r] = ld_stream_f4(a.w + e + 4);
           }
         }
+        if (PF) {
+          // the lane's first chunk past RND * G (segments longer than a unit covers) into L1
+          // now, so the extra-chunk loop of consume_unit does not wait on memory
+          const uint32_t c = gl + RND * G;
+          if (c < U.ln[u]) {
+            const uint64_t e = 8ull * (U.st[u] + c);
+            prefetch_l1(a.idx + e);
+            if (HAS_W) prefetch_l1(a.w + e);
+          }
+        }
       }
     };
     auto consume_unit = [&](const Unit& U) {
@@ -385,16 +395,6 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
     while (k < nslices) {
       fetch_desc(row2, mst, mn, mxv);                            // slice k + 2W
       row2 = fetch_row(k + 3 * nwarps, blk);                     // slice k + 3W
-      if (PF) {
-        // slice k + W into L2: one prefetch per 32-byte sector of the lane's segment
-        for (uint32_t c = 0; c < nn; c += 2) {
-          prefetch_l2(a.idx + 8ull * (nst + c));
-          if (HAS_W) {
-            prefetch_l2(a.w + 8ull * (nst + c));
-            prefetch_l2(a.w + 8ull * (nst + c) + 8);
-          }
-        }
-      }
       // This slice's units: the loads of the next unit (of this slice, or the first unit of
       // slice k + W) are issued before the current unit's atomics.
 #pragma unroll
@@ -550,7 +550,10 @@ static void tiled_config(double chunks, bool has_w, int32_t variant, int& G, int
   else if (chunks <= 5.0) { G = has_w ? 4 : 2; RND = has_w ? 1 : 2; }
   else if (chunks <= 9.0) { G = 8; RND = 1; }
   else { G = 8; RND = 2; }
-  PF = 0;  // measured: L2 prefetch of the next slice does not pay at 2-10 % event rates
+  // measured: prefetching a lane's first chunk past RND * G into L1 is neutral (30.3 against
+  // 31.0 us counts, 59.2 against 59.5 us weights at 2 %); an L2 prefetch of the next slice's
+  // segments, tried before it, was 5 % slower
+  PF = 0;
   if (variant > 0) {
     G = variant & 0xFF;
     RND = (variant >> 8) & 0xFF;

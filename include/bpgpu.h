@@ -195,7 +195,7 @@ typedef struct {
   int32_t n_tiles;    /* ceil(n / tile_w) */
   int32_t heter;      /* 1: the plan carries permuted float32 weights */
   int32_t variant;    /* tiled-kernel variant G | RND << 8 | PF << 16 (lanes per segment, chunk rounds,
-                         L2 prefetch), 0 = chosen from the mean segment length; set by the caller,
+                         L1 prefetch of a segment's extra chunks), 0 = chosen from the mean segment length; set by the caller,
                          e.g. after timing the candidates of bp_csr_plan_variants */
   uint64_t entries;   /* capacity of the padded index array */
   void* mem;          /* device memory holding the plan (caller-owned) */

@@ -215,8 +215,8 @@ def test_plan_cache_and_rowpar_agree(ev, orc, monkeypatch):
 
 @pytest.mark.parametrize("variant", ["1,1,0", "2,1,1", "4,1,0", "2,2,1", "8,1,1", "8,2,0"])
 def test_tiled_kernel_variants(bplib, orc, variant):
-  """The planned kernels in every compiled variant (lanes per segment, chunk rounds, L2
-  prefetch), on rows of uneven length including one far longer than a round.  Runs in a
+  """The planned kernels in every compiled variant (lanes per segment, chunk rounds, L1
+  prefetch of a segment's extra chunks), on rows of uneven length including one far longer than a round.  Runs in a
   child process (the variant is read once per process)."""
   import os
   import subprocess

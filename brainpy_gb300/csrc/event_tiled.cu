@@ -8,7 +8,7 @@
 //      columns.  CTA `rank` takes 1/R of the compaction blocks; for each active row it loads
 //      the row's segment for its tile (16-byte chunks of 8 tile-local uint16 indices) and adds
 //      into a shared-memory accumulator (uint32 counts for a homogeneous weight, float32
-//      otherwise), with the next rows' segments prefetched into L2.  At the end the R
+//      otherwise), with the next rows' segments in flight.  At the end the R
 //      accumulators of the cluster are summed through distributed shared memory and every
 //      output column is written exactly once.
 //
@@ -535,7 +535,7 @@ static bp_status launch_tiled_g(const TiledArgs& a, int R, cudaStream_t st) {
   return BP_OK;
 }
 
-// (lanes per segment, chunk rounds, L2 prefetch): the plan's chosen variant when set
+// (lanes per segment, chunk rounds, L1 prefetch of extra chunks): the plan's chosen variant when set
 // (bp_csr_plan.variant = G | RND << 8 | PF << 16, e.g. from an autotuning pass), otherwise
 // from the mean segment length in 16-byte chunks; BPGPU_TILED=G,RND,PF overrides both.
 static void tiled_config(double chunks, bool has_w, int32_t variant, int& G, int& RND, int& PF) {

@@ -959,34 +959,31 @@ bp_status bp_csrmv_planned_n(const bp_csr_plan* plan, const float* w_homo, const
   BP_REQUIRE(smem <= (size_t)max_smem_optin() - kStaticSmemReserve, BP_ENOTSUP,
              "csrmv_planned_n: tile of %d columns does not fit shared memory", plan->tile_w);
   PlanView v = plan_view(plan);
-  // row splits: enough CTAs for two per SM
   const int nt = plan->n_tiles;
-  int splits = (int)((2 * device_sm_count() + nt - 1) / nt);
-  if (splits < 1) splits = 1;
-  if ((int64_t)splits > m) splits = (int)m;
   float* part = static_cast<float*>(workspace);
   static bool configured[2][64] = {{false}};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) dev = 0;
-  ScopedKernelTimer tk(st);
-  if (homo) {
-    if (!configured[0][dev]) {
-      BP_CUDA_TRY(cudaFuncSetAttribute(csrmv_n_planned_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       max_smem_optin() - (int)kStaticSmemReserve));
-      configured[0][dev] = true;
-    }
-    csrmv_n_planned_kernel<false><<<nt * splits, 1024, smem, st>>>(v.seg_off, v.idx, nullptr, vec, m, n,
-                                                                   plan->tile_w, nt, splits, part);
-  } else {
-    if (!configured[1][dev]) {
-      BP_CUDA_TRY(cudaFuncSetAttribute(csrmv_n_planned_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       max_smem_optin() - (int)kStaticSmemReserve));
-      configured[1][dev] = true;
-    }
-    csrmv_n_planned_kernel<true><<<nt * splits, 1024, smem, st>>>(v.seg_off, v.idx, v.w, vec, m, n, plan->tile_w, nt,
-                                                                  splits, part);
+  auto kfn = homo ? csrmv_n_planned_kernel<false> : csrmv_n_planned_kernel<true>;
+  if (!configured[homo ? 0 : 1][dev]) {
+    BP_CUDA_TRY(
+        cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_optin() - (int)kStaticSmemReserve));
+    configured[homo ? 0 : 1][dev] = true;
   }
+  // row splits: as many CTAs as are resident at once (one wave), at least one per tile.  Every
+  // CTA walks the same number of rows, so a second partial wave would double the time.
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, 1024, smem) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  int splits = (int)(((int64_t)per_sm * device_sm_count()) / nt);
+  if (splits < 1) splits = 1;
+  if ((int64_t)splits > m) splits = (int)m;
+  ScopedKernelTimer tk(st);
+  kfn<<<nt * splits, 1024, smem, st>>>(v.seg_off, v.idx, homo ? nullptr : v.w, vec, m, n, plan->tile_w, nt, splits,
+                                       part);
   bp_status s = check_launch("csrmv_n_planned_kernel");
   if (s != BP_OK) return s;
   int64_t g = (m + 255) / 256;

@@ -43,13 +43,15 @@ def parse():
   ap.add_argument("--no-cpu-baseline", action="store_true")
   ap.add_argument("--cpu-seconds", type=float, default=12.0)
   ap.add_argument("--workload", default="event_csrmv",
-                  choices=["event_csrmv", "coba", "batched", "jitconn_net", "serve", "sweep", "vmap", "stdp"],
+                  choices=["event_csrmv", "coba", "batched", "jitconn_net", "serve", "sweep", "vmap", "stdp",
+                           "sparse_n"],
                   help="event_csrmv (headline); coba: the 4000-neuron COBA example; batched: 256 uneven "
                        "networks in persistent cluster launches vs the plain per-network path; jitconn_net: "
                        "4M-neuron just-in-time network; serve: continuous-batching serving loop; sweep: the "
                        "operator sweep (event/sparse csrmv, jitconn) as one JSON line; vmap: a batch of 8 "
                        "spike vectors through one matrix in one launch pair vs 8 sequential calls; stdp: the "
-                       "CSR layers' pre/post-spike weight updates")
+                       "CSR layers' pre/post-spike weight updates; sparse_n: sparse.csrmv transpose=False "
+                       "on a dense vector")
   ap.add_argument("--nets", type=int, default=256)
   ap.add_argument("--delay", type=float, default=None,
                   help="coba: synaptic delay (ms) of every projection, as FullProjAlignPostMg(delay=...)")
@@ -209,7 +211,7 @@ def main():
   args = parse()
   if args.workload != "event_csrmv":
     fn = {"coba": bench_coba, "batched": bench_batched, "jitconn_net": bench_jitconn_net, "serve": bench_serve,
-          "sweep": bench_sweep, "vmap": bench_vmap, "stdp": bench_stdp}
+          "sweep": bench_sweep, "vmap": bench_vmap, "stdp": bench_stdp, "sparse_n": bench_sparse_n}
     line = fn[args.workload](args)
     if line is not None:
       print(json.dumps(line))
@@ -699,6 +701,33 @@ def bench_stdp(args):
           "functional_copy": {"ms_per_step": t_copy * 1e3, "value": active * k / t_copy,
                               "note": "copies all nnz weights first, as the reference's kernel returns a new array"},
           "gpu_launches": 1}
+
+
+def bench_sparse_n(args):
+  """sparse.csrmv transpose=False, y = A x on a dense vector (brainpy/_src/math/sparse/_csr_mv.py:
+  29-108), at --n / --fanout on FixedProb rows: the tiled plan's row-gather kernel plus the
+  tile-order reduction.  Algorithmic bytes on the reference's CSR format: indptr, an int32
+  index per entry, the vector read and the output written."""
+  from brainpy_gb300.connect import fixed_prob_csr
+  from brainpy_gb300.math import sparse
+  n, k = args.n, args.fanout
+  ind, ptr = fixed_prob_csr(n, n, k, seed=0)
+  w = torch.ones(1, device="cuda")
+  x = torch.randn(n, device="cuda", generator=torch.Generator("cuda").manual_seed(4))
+  out = sparse.csrmv(w, ind, ptr, x, shape=(n, n), transpose=False)  # builds and caches the plan
+  flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+  t = _graph_time(lambda: sparse.csrmv(w, ind, ptr, x, shape=(n, n), transpose=False), flush_buf)
+  peak, _ = load_peaks()
+  nnz = ind.numel()
+  b = 4 * (n + 1) + 4 * nnz + 4 * n + 4 * n
+  return {"metric": "sparse.csrmv transpose=False (matrix entries/s)", "value": nnz / t, "unit": "entries/s",
+          "n_gpus": 1, "steps": 20, "warmup": 3, "ms_per_step": t * 1e3, "higher_is_better": True,
+          "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+          "config": {"workload": f"sparse_csrmv_N N={n} K={k} homo", "l2": "flushed before each replay",
+                     "timing": "CUDA-graph replay, CUDA events", "checksum": float(out.abs().sum())},
+          "roofline": {"bound": "hbm", "achieved": b / t / 1e9, "peak": peak, "unit": "GB/s",
+                       "frac": b / t / 1e9 / peak, "alg_bytes_per_launch": b},
+          "gpu_launches": 2}
 
 
 def launches_per_step(args):

@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(256) plan_build_kernel(const IdxT* __restrict_
       uint32_t h = hist[t], hp = (h + 7u) & ~7u;
       for (uint32_t p = h; p < hp; ++p) {
         uint64_t dst = rs + offs[t] + p;
-        idx[dst] = kPadIndex;
+        idx[dst] = (uint16_t)tile_w;  // the pad index: one past the tile
         if (w) w[dst] = 0.0f;
       }
     }
@@ -163,7 +163,7 @@ constexpr int tiled_threads() {
 }
 
 // Shared-memory reductions issued under a predicate (no branch): entries with index >= lim
-// are skipped -- the 0xFFFF padding, and every entry of a chunk given lim = 0.
+// are skipped -- the padding (index tile_w), and every entry of a chunk given lim = 0.
 __device__ __forceinline__ void red_if(uint32_t x, uint32_t lim, uint32_t addr, uint32_t v) {
   asm volatile("{\n\t.reg .pred p;\n\tsetp.lt.u32 p, %0, %1;\n\t@p red.shared.add.u32 [%2], %3;\n\t}" ::"r"(x),
                "r"(lim), "r"(addr), "r"(v));
@@ -624,15 +624,15 @@ __global__ void __launch_bounds__(1024) csrmv_n_planned_kernel(const uint32_t* _
                                                                const float* __restrict__ w, const float* __restrict__ x,
                                                                int64_t m, int64_t n, int32_t tile_w, int32_t n_tiles,
                                                                int32_t splits, float* __restrict__ part) {
-  extern __shared__ float xs[];
+  extern __shared__ float xs[];  // tile_w + 1: xs[tile_w] = 0 is what the pad index reads
   const int t = blockIdx.x % n_tiles;
   const int sp = blockIdx.x / n_tiles;
   const int64_t col0 = (int64_t)t * tile_w;
   for (int k = threadIdx.x; k < tile_w; k += blockDim.x) xs[k] = col0 + k < n ? __ldg(x + col0 + k) : 0.0f;
+  if (threadIdx.x == 0) xs[tile_w] = 0.0f;
   __syncthreads();
   const int64_t r0 = (int64_t)sp * m / splits, r1 = (int64_t)(sp + 1) * m / splits;
   const int64_t so_stride = (int64_t)n_tiles + 1;
-  const uint32_t lim = (uint32_t)tile_w;
   // groups of 4 lanes per row: a segment's chunks are read as one contiguous run; the next
   // row's segment bounds load while the current row is summed
   const int gl = threadIdx.x & 3;
@@ -660,13 +660,13 @@ __global__ void __launch_bounds__(1024) csrmv_n_planned_kernel(const uint32_t* _
         const float4 w0 = __ldg(reinterpret_cast<const float4*>(w + 8ull * c));
         const float4 w1 = __ldg(reinterpret_cast<const float4*>(w + 8ull * c + 4));
         const float ww[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+        // pad entries read xs[tile_w] = 0 with a zero weight: they add +0 (acc starts at +0
+        // and a sum of floats is never -0 unless every term is), no test needed
 #pragma unroll
-        for (int k = 0; k < 8; ++k)
-          if (q[k] < lim) acc = fmaf(ww[k], xs[q[k]], acc);
+        for (int k = 0; k < 8; ++k) acc = fmaf(ww[k], xs[q[k]], acc);
       } else {
 #pragma unroll
-        for (int k = 0; k < 8; ++k)
-          if (q[k] < lim) acc += xs[q[k]];
+        for (int k = 0; k < 8; ++k) acc += xs[q[k]];
       }
     }
     acc += __shfl_xor_sync(0xffffffffu, acc, 1);
@@ -955,7 +955,7 @@ bp_status bp_csrmv_planned_n(const bp_csr_plan* plan, const float* w_homo, const
   const size_t need = bp_csrmv_planned_n_workspace_size(plan);
   BP_REQUIRE(workspace && workspace_bytes >= need, BP_ENOMEM, "csrmv_planned_n: workspace %zu < %zu", workspace_bytes,
              need);
-  const size_t smem = sizeof(float) * (size_t)plan->tile_w;
+  const size_t smem = sizeof(float) * ((size_t)plan->tile_w + 1);
   BP_REQUIRE(smem <= (size_t)max_smem_optin() - kStaticSmemReserve, BP_ENOTSUP,
              "csrmv_planned_n: tile of %d columns does not fit shared memory", plan->tile_w);
   PlanView v = plan_view(plan);

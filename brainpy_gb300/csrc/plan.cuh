@@ -3,7 +3,9 @@
 // For a CSR matrix of shape m x n the output columns are cut into n_tiles tiles of
 // tile_w columns.  Every row's column indices are regrouped by tile; the group of
 // row r for tile t (a "segment") holds tile-local uint16 indices (col - t*tile_w) and
-// is padded with 0xFFFF to a multiple of 8 entries, so that every segment is a whole
+// is padded with the index tile_w (one past the tile: every kernel's `< tile_w` test skips
+// it, and a gather from a shared-memory tile with a zero at tile_w adds nothing) to a
+// multiple of 8 entries, so that every segment is a whole
 // number of 16-byte chunks starting on a 16-byte boundary (a valid bulk-copy source).
 // Heterogeneous weights are permuted along (float32, zero padding, same positions:
 // chunk c holds weights [8c, 8c + 8), 32 bytes).
@@ -23,8 +25,7 @@
 namespace bp {
 
 constexpr int kPlanMaxTiles = 4000;  // plan build keeps 3 x n_tiles words in 48 KB of shared memory
-constexpr int kPlanMaxTileW = 65535;  // local indices are uint16, 0xFFFF is the pad value
-constexpr uint16_t kPadIndex = 0xFFFF;
+constexpr int kPlanMaxTileW = 65535;  // local indices and the pad value tile_w are uint16
 constexpr int kChunkEntries = 8;      // entries per 16-byte chunk
 
 // Byte offsets of the arrays inside the plan memory.

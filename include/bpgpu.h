@@ -216,7 +216,7 @@ bp_status bp_csr_plan_build(const float* data, int64_t ndata, const void* indice
                             size_t bytes, bp_csr_plan* plan_out, bp_stream_t stream);
 
 /* device arrays inside a plan: seg_off[m][n_tiles+1] (segment t of row r is the 16-byte chunks
- * [seg_off[r][t], seg_off[r][t+1]) of idx, 8 tile-local indices each, 0xFFFF padding),
+ * [seg_off[r][t], seg_off[r][t+1]) of idx, 8 tile-local indices each, padded with the index tile_w),
  * idx[entries], w[entries] or NULL */
 bp_status bp_csr_plan_arrays(const bp_csr_plan* plan, const uint32_t** seg_off, const uint16_t** idx,
                              const float** w);

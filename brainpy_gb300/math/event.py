@@ -13,10 +13,11 @@ from typing import Optional, Tuple, Union
 import torch
 
 from .. import _lib
+from .. import tuning
 from . import _grad
 from ._utils import as_tensor, default_device, event_type, float_data, index_type
 
-__all__ = ["csrmv", "csrmv_taichi", "csrmv_batch", "info", "CSRPlan", "prepare"]
+__all__ = ["csrmv", "csrmv_taichi", "csrmv_batch", "info", "CSRPlan", "prepare", "autotune"]
 
 
 class CSRPlan:
@@ -221,8 +222,11 @@ def prepare(indices, indptr, *, shape, data=None, tile_w=None, cluster=4) -> CSR
 
 # ---- automatic plan cache ---------------------------------------------------------
 # Keyed by the identity and version counter of the CSR tensors (and of heterogeneous
-# weights), so an in-place change of any of them invalidates the entry.
+# weights), so an in-place change of any of them invalidates the entry.  _ROUTES holds, under
+# the same keys, the kernel family `autotune` chose for a matrix ("row" or "tiled"); a matrix
+# without a route takes the tiled plan from the size thresholds below.
 _PLANS = {}
+_ROUTES = {}
 _PLAN_MIN_N = int(os.environ.get("BPGPU_PLAN_MIN_N", 1 << 15))
 _PLAN_MIN_NNZ = int(os.environ.get("BPGPU_PLAN_MIN_NNZ", 1 << 20))
 _PLAN_DISABLE = os.environ.get("BPGPU_DISABLE_PLAN", "0") == "1"
@@ -232,14 +236,46 @@ def _plan_key(t):
   return (id(t), t.data_ptr(), t._version)
 
 
-def _cached_plan(data, indices, indptr, shape):
+def _matrix_key(data, indices, indptr, m, n):
+  heter = data.numel() > 1
+  return (_plan_key(indices), _plan_key(indptr), int(m), int(n), _plan_key(data) if heter else None)
+
+
+def _matrix_refs(data, indices, indptr):
+  return [weakref.ref(indices), weakref.ref(indptr)] + ([weakref.ref(data)] if data.numel() > 1 else [])
+
+
+def _route(data, indices, indptr, shape):
+  """The autotuned kernel family of this matrix: "row", "tiled", or None (not tuned)."""
+  if not _ROUTES:
+    return None
+  key = _matrix_key(data, indices, indptr, shape[0], shape[1])
+  ent = _ROUTES.get(key)
+  if ent is None:
+    return None
+  refs, route = ent
+  if all(r() is not None for r in refs):
+    return route
+  del _ROUTES[key]
+  return None
+
+
+def _cached_plan(data, indices, indptr, shape, force=False, routed=True):
+  """The plan of this matrix (built on first use), or None when the matrix is below the
+  size thresholds, plans are disabled, or the autotuner routed its event product to the row
+  kernel.  `force` builds one below the thresholds (an autotuned "tiled" route, or tuning
+  itself); `routed=False` ignores the event product's route (the dense-vector products)."""
   if _PLAN_DISABLE:
     return None
   m, n = int(shape[0]), int(shape[1])
-  if n < _PLAN_MIN_N or indices.numel() < _PLAN_MIN_NNZ:
-    return None
+  if not force:
+    route = _route(data, indices, indptr, (m, n)) if routed else None
+    if route == "row":
+      return None
+    if route is None and (n < _PLAN_MIN_N or indices.numel() < _PLAN_MIN_NNZ):
+      return None
   heter = data.numel() > 1
-  key = (_plan_key(indices), _plan_key(indptr), m, n, _plan_key(data) if heter else None)
+  key = _matrix_key(data, indices, indptr, m, n)
   ent = _PLANS.get(key)
   if ent is not None:
     refs, plan = ent
@@ -249,9 +285,85 @@ def _cached_plan(data, indices, indptr, shape):
   for k in [k for k, (refs, _) in _PLANS.items() if any(r() is None for r in refs)]:
     del _PLANS[k]
   plan = CSRPlan(indices, indptr, (m, n), data if heter else None)
-  refs = [weakref.ref(indices), weakref.ref(indptr)] + ([weakref.ref(data)] if heter else [])
-  _PLANS[key] = (refs, plan)
+  _PLANS[key] = (_matrix_refs(data, indices, indptr), plan)
   return plan
+
+
+def _valid_choice(choice):
+  if choice == "row":
+    return True
+  if not isinstance(choice, str) or not choice.startswith("tiled:"):
+    return False
+  try:
+    return int(choice.split(":", 1)[1]) in CSRPlan.variants()
+  except ValueError:
+    return False
+
+
+def autotune(data, indices, indptr, events, *, shape: Tuple[int, int], transpose: bool = True,
+             reps: int = 10, cache: Optional[tuning.TuneCache] = None, timer=None,
+             float_rule=_lib.BP_EV_F32_POS) -> dict:
+  """Chooses the kernel family for this matrix at the firing rate of `events` (a spike vector
+  representative of the model) and keeps the choice for later ``csrmv`` calls on the same
+  arrays: the row-parallel kernel, or the column-tiled plan in one of its compiled variants.
+
+  Every candidate is timed on `events` (``reps`` calls after two warm-up calls, CUDA events)
+  unless `cache` (default: the process cache, file-backed when ``BPGPU_TUNE_CACHE`` is set)
+  already holds a record for the same device, sizes, weight kind, event type and half-octave
+  rate bucket.  Returns the record: ``{"choice": "row" | "tiled:<variant>", "times_us":
+  {...}, "rate": r}``.  Every candidate computes the same product (bit for bit with a
+  homogeneous weight), so the choice changes speed only.  With ``transpose=False`` only the
+  row-parallel family exists and nothing is timed."""
+  dev = events.device if isinstance(events, torch.Tensor) and events.is_cuda else default_device()
+  d = float_data(data, dev)
+  indices = as_tensor(indices, dev)
+  indptr = as_tensor(indptr, dev)
+  events = as_tensor(events, dev)
+  _check_common(d, indices, indptr, events, shape, bool(transpose))
+  if index_type(indptr, "indptr") != index_type(indices, "indices"):
+    raise ValueError("indices and indptr must have the same integer type.")
+  m, n = int(shape[0]), int(shape[1])
+  if not transpose:
+    return {"choice": "row", "times_us": {}, "rate": None}
+  etype, ev = event_type(events, float_rule)
+  if etype == _lib.BP_EV_BOOL:
+    active = int(ev.sum())
+  elif etype == _lib.BP_EV_F32_POS:
+    active = int((ev > 0).sum())
+  else:
+    active = int((ev != 0).sum())
+  rate = active / max(m, 1)
+  heter = d.numel() > 1
+  key = tuning.make_key("event_csrmv_T", torch.cuda.get_device_name(dev), m, n, indices.numel(), heter, etype,
+                        tuning.rate_bucket(rate))
+  cache = cache if cache is not None else tuning.default_cache()
+  rec = cache.lookup(key)
+  if rec is not None and not _valid_choice(rec.get("choice")):
+    rec = None  # a record from a build with other variants: time again
+  if rec is None:
+    out = torch.empty(n, dtype=torch.float32, device=dev)
+    cands = {"row": lambda: _event_csrmv(d, indices, indptr, events, shape, True, float_rule, out=out, use_plan=False)}
+    plan = _cached_plan(d, indices, indptr, (m, n), force=True)
+    if plan is not None:
+      w = None if plan.heter else d
+      for code in CSRPlan.variants():
+        def run(code=code):
+          plan.variant = code
+          return plan.csrmv(events, w, out=out, float_rule=float_rule)
+        cands[f"tiled:{code}"] = run
+    best, times = tuning.pick(cands, timer or tuning.cuda_timer(reps))
+    rec = {"choice": best, "times_us": times, "rate": rate}
+    cache.store(key, rec)
+    cache.save()
+  mkey = _matrix_key(d, indices, indptr, m, n)
+  if rec["choice"] == "row" or _PLAN_DISABLE:
+    _ROUTES[mkey] = (_matrix_refs(d, indices, indptr), "row")
+    _PLANS.pop(mkey, None)  # the row kernel needs no plan: release its memory
+  else:
+    plan = _cached_plan(d, indices, indptr, (m, n), force=True)
+    plan.variant = int(rec["choice"].split(":", 1)[1])
+    _ROUTES[mkey] = (_matrix_refs(d, indices, indptr), "tiled")
+  return rec
 
 
 def _check_common(data, indices, indptr, events, shape, transpose):
@@ -292,7 +404,7 @@ def _event_csrmv(data, indices, indptr, events, shape, transpose, float_rule, ou
   m, n = int(shape[0]), int(shape[1])
   n_out = n if transpose else m
   if transpose and use_plan:
-    plan = _cached_plan(data, indices, indptr, (m, n))
+    plan = _cached_plan(data, indices, indptr, (m, n), force=_route(data, indices, indptr, (m, n)) == "tiled")
     if plan is not None:
       return plan.csrmv(events, None if plan.heter else data, out=out, float_rule=float_rule)
   if out is None:
@@ -361,7 +473,7 @@ def csrmv_batch(data, indices, indptr, events, *, shape: Tuple[int, int], transp
     _check_common(d, indices, indptr, events[0], shape, True)
     if index_type(indptr, "indptr") != index_type(indices, "indices"):
       raise ValueError("indices and indptr must have the same integer type.")
-    plan = _cached_plan(d, indices, indptr, (m, n))
+    plan = _cached_plan(d, indices, indptr, (m, n), force=_route(d, indices, indptr, (m, n)) == "tiled")
     if plan is not None:
       return plan.csrmv_batch(events, None if plan.heter else d, float_rule=float_rule)
   out = torch.empty((events.shape[0], n if transpose else m), dtype=torch.float32, device=dev)

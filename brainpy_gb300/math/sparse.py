@@ -43,7 +43,7 @@ def _csrmv(data, indices, indptr, vector, shape, transpose, out=None, use_plan=T
   if index_type(indptr, "indptr") != itype:
     raise ValueError("indices and indptr must have the same integer type.")
   if use_plan:
-    plan = _event._cached_plan(data, indices, indptr, (m, n))
+    plan = _event._cached_plan(data, indices, indptr, (m, n), routed=False)
     if plan is not None:
       if transpose:
         return plan.sparse_t(vector, None if plan.heter else data, out=out)
@@ -113,7 +113,7 @@ def csrmv_batch(data, indices, indptr, vectors, *, shape: Tuple[int, int], trans
       raise ValueError(f"Shape mismatch, vec ({vectors.shape[1]},) and mat {tuple(shape)} with transpose=True.")
     if d.shape[0] not in (1, indices.shape[0]):
       raise ValueError("The size of data should be 1 or be consistent with indices.")
-    plan = _event._cached_plan(d, indices, indptr, (m, n))
+    plan = _event._cached_plan(d, indices, indptr, (m, n), routed=False)
     if plan is not None:
       return plan.sparse_t_batch(vectors, None if plan.heter else d)
   out = torch.empty((vectors.shape[0], n if transpose else m), dtype=torch.float32, device=dev)

@@ -252,6 +252,49 @@ def test_plan_autotune_and_every_variant(ev, orc):
     plan.csrmv(e, w)
 
 
+def test_autotune_routes_row_or_tiled(ev, orc, tmp_path):
+  """event.autotune times the row-parallel kernel against every tiled variant, keeps the
+  winner for the matrix, and later csrmv calls follow it; a cached record is applied without
+  timing (a forced "row" record means no plan is held); results are the oracle's counts."""
+  from brainpy_gb300 import tuning
+  from brainpy_gb300.connect import fixed_prob_csr
+  n, k = 40000, 100  # below the plan size thresholds: untuned calls take the row kernel
+  ind, ptr = fixed_prob_csr(n, n, k, seed=9)
+  rng = np.random.default_rng(10)
+  events = rng.random(n) < 0.02
+  e = torch.as_tensor(events, device="cuda")
+  w = torch.tensor([0.5], device="cuda")
+  want = orc.event_csrmv(np.float32(0.5), ind.cpu().numpy(), ptr.cpu().numpy(), events, (n, n), True)["count32"]
+  cache = tuning.TuneCache(str(tmp_path / "tune.json"))
+  rec = ev.autotune(w, ind, ptr, e, shape=(n, n), cache=cache, reps=3)
+  codes = ev.CSRPlan.variants()
+  assert set(rec["times_us"]) == {"row"} | {f"tiled:{c}" for c in codes}
+  assert rec["choice"] == min(rec["times_us"], key=rec["times_us"].get)
+  assert abs(rec["rate"] - events.mean()) < 1e-12
+  key = ev._matrix_key(w, ind, ptr, n, n)
+  assert ev._ROUTES[key][1] == ("row" if rec["choice"] == "row" else "tiled")
+  assert (key in ev._PLANS) == (rec["choice"] != "row")
+  np.testing.assert_array_equal(ev.csrmv(w, ind, ptr, e, shape=(n, n), transpose=True).cpu().numpy(), want)
+  # the record was saved; a fresh cache reads it, and a forced record is applied as is
+  again = tuning.TuneCache(str(tmp_path / "tune.json"))
+  assert len(again.entries) == 1
+  (rk, _), = again.entries.items()
+  for forced in ["tiled:" + str(codes[0]), "row"]:
+    again.store(rk, {"choice": forced, "times_us": {}, "rate": rec["rate"]})
+    got = ev.autotune(w, ind, ptr, e, shape=(n, n), cache=again)
+    assert got["choice"] == forced and got["times_us"] == {}
+    assert ev._ROUTES[key][1] == forced.split(":")[0]
+    assert (key in ev._PLANS) == (forced != "row")
+    if forced != "row":
+      assert ev._PLANS[key][1].variant == codes[0]
+    np.testing.assert_array_equal(ev.csrmv(w, ind, ptr, e, shape=(n, n), transpose=True).cpu().numpy(), want)
+    np.testing.assert_array_equal(
+        ev.csrmv_batch(w, ind, ptr, e[None], shape=(n, n), transpose=True)[0].cpu().numpy(), want)
+  # transpose=False has one family: nothing is timed
+  assert ev.autotune(w, ind, ptr, e, shape=(n, n), transpose=False)["choice"] == "row"
+  ev._ROUTES.pop(key, None)
+
+
 @pytest.mark.parametrize("n,evkind", [(200_000, "bool"), (1_000_000, "float"), (2_000_000, "bool")])
 def test_non_transpose_bits_path(ev, orc, n, evkind):
   """transpose=0 with the event vector as bits in shared memory (n <= 1.6M), and beyond it

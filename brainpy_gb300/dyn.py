@@ -14,7 +14,7 @@ Two execution forms:
 """
 import ctypes
 import math
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from typing import Optional
 
 import numpy as np

@@ -20,7 +20,7 @@ A job's result does not depend on what it shares the device with: every path is 
 """
 import math
 import time
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from typing import List, Optional
 
 import numpy as np

@@ -7,7 +7,6 @@ f(outdim_parallel=False, transpose=True)" (_matvec_taichi.py:270-279).  These te
 that holds: exactly for the Taichi CPU connectivity (one stream per owner over the whole other
 dimension), and not for the Taichi GPU connectivity, whose 32 lanes per owner split a width
 computed from the owner count."""
-import numpy as np
 import pytest
 
 

@@ -368,7 +368,7 @@ def main():
           "kernel": "event_csrmv: compact_blocked_kernel + ecsr_t_tiled_kernel (the call's two kernels, one bracket)",
           "timing": "CUDA events around one CUDA-graph replay of all timed calls, back to back",
           "alg_bytes_per_launch": b_alg, "kernel_ms": kernel_ms,
-          "traffic": profile_traffic(f"event_csrmv_N1e6_K1000_r2_{args.weights}.md")}
+          "traffic": profile_traffic(f"event_csrmv_N1e6_K1000_rate2pct_{args.weights}.md")}
   line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
           "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
           "dtype": "f32", "data": "synthetic",

@@ -365,7 +365,9 @@ def main():
   achieved = b_alg / (kernel_ms * 1e-3) / 1e9
   roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
           "peak_kind": peak_kind,
-          "kernel": "event_csrmv: compact_blocked_kernel + ecsr_t_tiled_kernel (the call's two kernels, one bracket)",
+          "kernel": ("event_csrmv: compact_blocked_kernel + ecsr_t_split_kernel + split_reduce_kernel (the call's "
+                     "three kernels, one bracket)" if launches_per_step(args) == 3 else
+                     "event_csrmv: compact_blocked_kernel + ecsr_t_tiled_kernel (the call's two kernels, one bracket)"),
           "timing": "CUDA events around one CUDA-graph replay of all timed calls, back to back",
           "alg_bytes_per_launch": b_alg, "kernel_ms": kernel_ms,
           "traffic": profile_traffic(f"event_csrmv_N1e6_K1000_rate2pct_{args.weights}.md")}
@@ -731,9 +733,12 @@ def bench_sparse_n(args):
 
 
 def launches_per_step(args):
-  """Kernels of ours per event.csrmv transpose call on the tiled plan (the path the
-  front-end takes for this size): blocked spike compaction + tiled accumulation."""
-  return 2
+  """Kernels of ours per event.csrmv transpose call.  A homogeneous weight on >= 2^19 columns
+  runs the counting plan: blocked spike compaction, split accumulation (16-bit counters), and
+  the reduction of the partial counts; per-synapse weights run the general plan: compaction
+  and the cluster-tiled accumulation."""
+  from brainpy_gb300.math import event
+  return 3 if (args.weights == "homo" and args.n >= event._SPLIT_MIN_N) else 2
 
 
 if __name__ == "__main__":

@@ -58,6 +58,7 @@ SIGNATURES = {
     "bp_jitconn_dense": (_c_i32, [_c_i32, _c_f32, _c_f32, _c_i32, _c_u32, _c_i64, _c_i64, _c_i32, _c_i32, _c_ptr,
                                   _c_ptr]),
     "bp_csr_plan_default_tile": (_c_i32, [_c_i64, _c_i32]),
+    "bp_csr_plan_count_tile": (_c_i32, [_c_i64]),
     "bp_csr_plan_variants": (_c_i32, [_c_ptr, _c_i32]),
     "bp_csr_plan_bytes": (_c_size, [_c_i64, _c_i64, _c_i64, _c_i32, _c_i32]),
     "bp_csr_plan_build": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_i32, _c_ptr,

@@ -18,6 +18,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <cstdio>
 #include <cstdlib>
 
@@ -42,12 +43,16 @@ template <typename IdxT>
 __global__ void __launch_bounds__(256) plan_build_kernel(const IdxT* __restrict__ indptr, const IdxT* __restrict__ indices,
                                                          const float* __restrict__ data, int64_t nnz, int64_t m,
                                                          int64_t n, int tile_w, int nt, uint32_t* __restrict__ seg_off,
-                                                         uint16_t* __restrict__ idx, float* __restrict__ w) {
+                                                         uint16_t* __restrict__ idx, float* __restrict__ w,
+                                                         uint32_t* __restrict__ meta) {
   extern __shared__ uint32_t sm[];
   uint32_t* hist = sm;               // nt
   uint32_t* offs = sm + nt;          // nt + 1
   uint32_t* cursor = offs + nt + 1;  // nt
+  uint32_t* tab = cursor + nt;       // 2 * kPlanDupCheckMax: open-addressing set of a row's columns
+  __shared__ int s_dup;
   const uint64_t per_row = 8ull * (uint64_t)nt + 8ull;
+  for (int i = threadIdx.x; i < 2 * kPlanDupCheckMax; i += blockDim.x) tab[i] = 0xFFFFFFFFu;
   for (int64_t row = blockIdx.x; row < m; row += gridDim.x) {
     int64_t b = (int64_t)indptr[row], e = (int64_t)indptr[row + 1];
     b = b < 0 ? 0 : (b > nnz ? nnz : b);
@@ -56,6 +61,37 @@ __global__ void __launch_bounds__(256) plan_build_kernel(const IdxT* __restrict_
     for (int t = threadIdx.x; t < nt; t += blockDim.x) {
       hist[t] = 0;
       cursor[t] = 0;
+    }
+    if (threadIdx.x == 0) {
+      s_dup = 0;
+      atomicMax(&meta[1], (uint32_t)(e - b));
+    }
+    __syncthreads();
+    // repeated columns: every in-range column of the row goes into a set of at least twice the
+    // row's length (a power of two); a column found already present is a repeat.  Rows longer
+    // than kPlanDupCheckMax are not checked and count as having repeats.
+    if (e - b > kPlanDupCheckMax) {
+      if (threadIdx.x == 0) meta[0] = 0u;
+    } else if (e - b > 1) {
+      uint32_t tsz = 64;
+      while (tsz < 2u * (uint32_t)(e - b)) tsz <<= 1;
+      const uint32_t mask = tsz - 1;
+      for (int64_t j = b + threadIdx.x; j < e; j += blockDim.x) {
+        const int64_t c = (int64_t)indices[j];
+        if (c < 0 || c >= n) continue;
+        uint32_t h = ((uint32_t)c * 2654435761u) & mask;
+        for (uint32_t probe = 0; probe < tsz; ++probe, h = (h + 1) & mask) {
+          const uint32_t old = atomicCAS(&tab[h], 0xFFFFFFFFu, (uint32_t)c);
+          if (old == 0xFFFFFFFFu) break;
+          if (old == (uint32_t)c) {
+            s_dup = 1;
+            break;
+          }
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x == 0 && s_dup) meta[0] = 0u;
+      for (uint32_t i = threadIdx.x; i < tsz; i += blockDim.x) tab[i] = 0xFFFFFFFFu;
     }
     __syncthreads();
     for (int64_t j = b + threadIdx.x; j < e; j += blockDim.x) {
@@ -475,6 +511,318 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
   cluster.sync();
 }
 
+// ---------------------------------------------------------------------------
+// split accumulation for large column tiles (homogeneous weight, events)
+// ---------------------------------------------------------------------------
+// DRAM serves random reads of up to ~128 bytes at a fixed rate of row activations, so the
+// number of segment reads a call makes sets its floor.  Tiles of up to 65,472 columns halve
+// that number against the cluster path's ~28K-column tiles (a row's segment for a tile is
+// ~125 bytes at fan-out 1000 and 16 tiles), but such a tile fits shared memory only as 16-bit
+// counters (two columns per 32-bit word, 125 KB).  CTA (tile t, split q) accumulates the
+// active rows of compaction blocks [q nb / R, (q + 1) nb / R) and writes its counts to the
+// workspace; split_reduce_kernel then adds the R partial counts of every column and writes
+// (float)count * w.
+//   - 16-bit counters are exact while no column gets 65,536 adds from one CTA: the plan has no
+//     repeated column in any row (plan meta[0]) and the CTA sees at most 65,535 active rows.
+//     Otherwise the CTA runs two passes over its rows with 32-bit counters, one for each half
+//     of the tile, and marks its partial as 32-bit.
+//   - The loop distributes a slice's chunks flat over the warp (chunk 32j + l of the slice's
+//     segments to lane l in round j), so every round but a slice's last keeps all lanes busy
+//     whatever the segment lengths; the loads of the next rounds are in flight while a round's
+//     shared-memory adds issue.
+constexpr int kSplitMaxTile = 65472;  // a multiple of 64 below the uint16 range
+constexpr int kSplitMaxSplits = 16;
+constexpr int kSplitRounds = 2;       // rounds of loads in flight
+
+struct SplitArgs {
+  const uint32_t* seg_off;
+  const uint16_t* idx;
+  const uint32_t* meta;
+  const int32_t* lists;
+  const int32_t* counts;
+  uint32_t* part;  // [n_tiles * R][tile_w] words: 16-bit pairs in the first tile_w / 2, or 32-bit counts
+  uint32_t* fmt;   // [n_tiles * R]: 0 = 16-bit pairs, 1 = 32-bit counts
+  int64_t m, n;
+  int32_t tile_w, n_tiles, nb, R;
+};
+
+__global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const SplitArgs a) {
+  constexpr unsigned FULL = 0xffffffffu;
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint32_t* acc = reinterpret_cast<uint32_t*>(smem);
+  const uint32_t acc_s = (uint32_t)__cvta_generic_to_shared(acc);
+  const int half_w = a.tile_w >> 1;  // words of the accumulator: 16-bit pairs, or one half in 32 bits
+  int* s_boff = reinterpret_cast<int*>(smem + sizeof(uint32_t) * (size_t)half_w);  // kBlockGroup + 1
+  __shared__ int s_wsum[32];
+  const int tile = blockIdx.x / a.R, q = blockIdx.x % a.R;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
+  const uint32_t tile_w = (uint32_t)a.tile_w;
+  const int64_t so_stride = a.n_tiles + 1;
+
+  auto zero_acc = [&]() {
+    uint4* acc4 = reinterpret_cast<uint4*>(acc);
+    for (int i = tid; i < (half_w >> 2); i += nthr) acc4[i] = make_uint4(0u, 0u, 0u, 0u);
+  };
+  zero_acc();
+  const int b0 = (int)((int64_t)q * a.nb / a.R), b1 = (int)((int64_t)(q + 1) * a.nb / a.R);
+
+  // the compaction kernel of this call may still be running (programmatic dependent launch)
+  cudaGridDependencySynchronize();
+
+  // exclusive prefix of the active-row counts of blocks [g0, g0 + ng) into s_boff; returns the total
+  auto group_prefix = [&](int g0, int ng) -> int {
+    __syncthreads();  // s_boff / s_wsum of an earlier use are no longer read
+    int v = tid < ng ? __ldg(a.counts + g0 + tid) : 0;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int t = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (lane == 31) s_wsum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      int t = lane < nwarps ? s_wsum[lane] : 0, ti = t;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int u = __shfl_up_sync(FULL, ti, o);
+        if (lane >= o) ti += u;
+      }
+      s_wsum[lane] = ti - t;
+    }
+    __syncthreads();
+    if (tid < ng) s_boff[tid] = s_wsum[warp] + incl - v;
+    if (tid == ng - 1) s_boff[ng] = s_wsum[warp] + incl;
+    __syncthreads();
+    return s_boff[ng];
+  };
+  // active rows of the whole split (several groups)
+  auto split_rows = [&]() -> int {
+    int my = 0;
+    for (int b = b0 + tid; b < b1; b += nthr) my += __ldg(a.counts + b);
+    my = warp_sum(my);
+    __syncthreads();
+    if (lane == 0) s_wsum[warp] = my;
+    __syncthreads();
+    int t = 0;
+    for (int i = 0; i < nwarps; ++i) t += s_wsum[i];
+    return t;
+  };
+
+  const bool one_group = b1 - b0 <= nthr;
+  const int rows = one_group ? (b1 > b0 ? group_prefix(b0, b1 - b0) : 0) : split_rows();
+  const bool packed = __ldg(a.meta) != 0u && rows <= 65535;
+  uint32_t* __restrict__ part = a.part + (size_t)blockIdx.x * (size_t)a.tile_w;
+
+  // one group of compaction blocks: the warp's slices k = warp, warp + W, ..., flat rounds
+  auto run_group = [&](int g0, int total, auto pk, uint32_t lo) {
+    constexpr bool PACK = decltype(pk)::value;
+    const int nslices = (total + 31) >> 5;
+    if (nslices == 0) return;
+    const int gmax = max(total - 1, 0);
+    const int ng = min(nthr, b1 - g0);
+    auto block_of = [&](int g) -> int {
+      int l = 0, h = ng;
+      while (h - l > 1) {
+        const int mid = (l + h) >> 1;
+        if (s_boff[mid] <= g) l = mid;
+        else h = mid;
+      }
+      return l;
+    };
+    auto fetch_row = [&](int k, int& blk) -> int32_t {
+      const int g = (k << 5) + lane;
+      if (k >= nslices || g >= total) return -1;
+      while (s_boff[blk + 1] <= g) ++blk;
+      return __ldg(a.lists + (int64_t)(g0 + blk) * kCompactRows + (g - s_boff[blk]));
+    };
+    auto fetch_desc = [&](int32_t row, uint32_t& st, uint32_t& nch) {
+      st = 0;
+      nch = 0;
+      if (row >= 0) {
+        const uint32_t* so = a.seg_off + (int64_t)row * so_stride + tile;
+        st = __ldg(so);
+        nch = __ldg(so + 1) - st;
+      }
+    };
+    const uint32_t lane_le = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
+    uint32_t s_d = 0, s_P = 0, s_C = 0, s_E = 0, s_n1 = 0, g_j = 0, g_base = 0;
+    auto prepare = [&](int kk, uint32_t st, uint32_t n) {
+      const bool valid = (kk << 5) + lane < total;
+      const uint32_t n1 = valid ? max(n, 1u) : 0u;
+      uint32_t incl = n1;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+      }
+      s_C = __shfl_sync(FULL, incl, 31);
+      s_P = incl - n1;
+      s_d = st - s_P;
+      s_n1 = n1;
+      s_E = __ballot_sync(FULL, valid && n == 0u);
+      g_j = 0;
+      g_base = 0;
+    };
+    int k = warp;
+    int blk = block_of(min((k << 5) + lane, gmax));
+    uint32_t nst, nn;
+    {
+      uint32_t st0, n0;
+      fetch_desc(fetch_row(k, blk), st0, n0);            // slice k
+      fetch_desc(fetch_row(k + nwarps, blk), nst, nn);   // slice k + W
+      prepare(k, st0, n0);
+    }
+    int32_t row2 = fetch_row(k + 2 * nwarps, blk);     // slice k + 2W
+    bool live = k < nslices;
+    // the next round of the warp's stream (moving on to slice k + W when slice k is done): the
+    // chunk is loaded (or zero with lim = 0); false once every slice of the warp is distributed
+    auto load_rd = [&](uint4& v, uint32_t& lim) -> bool {
+      while (live && (g_j << 5) >= s_C) {
+        k += nwarps;
+        if (k >= nslices) {
+          live = false;
+          break;
+        }
+        prepare(k, nst, nn);
+        fetch_desc(row2, nst, nn);                      // slice k + W
+        row2 = fetch_row(k + 2 * nwarps, blk);          // slice k + 2W
+      }
+      v = make_uint4(0u, 0u, 0u, 0u);
+      lim = 0u;
+      if (!live) return false;
+      const uint32_t g = (g_j << 5) + lane;
+      const uint32_t contrib = ((s_P >> 5) == g_j && s_n1 > 0u) ? (1u << (s_P & 31u)) : 0u;
+      const uint32_t M = __reduce_or_sync(FULL, contrib);
+      const int o = ((int)(g_base + __popc(M & lane_le)) - 1) & 31;
+      g_base += __popc(M);
+      ++g_j;
+      const uint32_t dd = __shfl_sync(FULL, s_d, o);
+      if (g < s_C) {
+        lim = ((s_E >> o) & 1u) ? 0u : 1u;
+        v = ld_stream_u4(a.idx + 8ull * (g + dd));
+      }
+      return true;
+    };
+    auto add8 = [&](const uint4 v, uint32_t lim) {
+      const uint32_t x[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
+                             v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        if (PACK) {
+          // two columns a word: column x adds 1 to the low half (x even) or high half (x odd)
+          red_if(x[e], lim ? tile_w : 0u, acc_s + ((x[e] >> 1) << 2), (x[e] & 1u) ? 0x10000u : 1u);
+        } else {
+          const uint32_t y = x[e] - lo;  // columns [lo, lo + half_w) of this pass; the pad falls outside
+          red_if(y, lim ? (uint32_t)half_w : 0u, acc_s + (y << 2), 1u);
+        }
+      }
+    };
+    uint4 v[kSplitRounds + 1];
+    uint32_t lim[kSplitRounds + 1];
+    bool ok[kSplitRounds + 1];
+#pragma unroll
+    for (int i = 0; i < kSplitRounds; ++i) ok[i] = load_rd(v[i], lim[i]);
+    while (ok[0]) {
+      ok[kSplitRounds] = load_rd(v[kSplitRounds], lim[kSplitRounds]);
+      add8(v[0], lim[0]);
+#pragma unroll
+      for (int i = 0; i < kSplitRounds; ++i) {
+        v[i] = v[i + 1];
+        lim[i] = lim[i + 1];
+        ok[i] = ok[i + 1];
+      }
+    }
+  };
+  auto run_split = [&](auto pk, uint32_t lo) {
+    for (int g0 = b0; g0 < b1; g0 += nthr) {
+      const int total = one_group ? rows : group_prefix(g0, min(nthr, b1 - g0));
+      run_group(g0, total, pk, lo);
+    }
+  };
+
+  if (packed) {
+    run_split(std::true_type{}, 0u);
+    __syncthreads();
+    const uint4* acc4 = reinterpret_cast<const uint4*>(acc);
+    uint4* p4 = reinterpret_cast<uint4*>(part);
+    for (int i = tid; i < (half_w >> 2); i += nthr) p4[i] = acc4[i];
+  } else {
+    for (int pass = 0; pass < 2; ++pass) {
+      const uint32_t lo = (uint32_t)(pass * half_w);
+      run_split(std::false_type{}, lo);
+      __syncthreads();
+      const uint4* acc4 = reinterpret_cast<const uint4*>(acc);
+      uint4* p4 = reinterpret_cast<uint4*>(part + lo);
+      for (int i = tid; i < (half_w >> 2); i += nthr) p4[i] = acc4[i];
+      if (pass == 0) {
+        __syncthreads();
+        zero_acc();
+        __syncthreads();
+      }
+    }
+  }
+  if (tid == 0) a.fmt[blockIdx.x] = packed ? 0u : 1u;
+}
+
+// out[t * tile_w + c] = (float)(sum over the R splits of tile t of their count of column c) * w,
+// eight columns a thread
+__global__ void __launch_bounds__(256) split_reduce_kernel(const uint32_t* __restrict__ part,
+                                                           const uint32_t* __restrict__ fmt,
+                                                           const float* __restrict__ w_homo, float* __restrict__ out,
+                                                           int64_t n, int32_t tile_w, int32_t n_tiles, int32_t R,
+                                                           int32_t vec_out) {
+  cudaGridDependencySynchronize();  // the partial counts of this call
+  const float w = __ldg(w_homo);
+  const int gpt = tile_w >> 3;
+  const int64_t groups = (int64_t)n_tiles * gpt;
+  for (int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gid < groups;
+       gid += (int64_t)gridDim.x * blockDim.x) {
+    const int t = (int)(gid / gpt);
+    const int c8 = (int)(gid - (int64_t)t * gpt) << 3;
+    const int64_t gc = (int64_t)t * tile_w + c8;
+    if (gc >= n) continue;
+    uint32_t s[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+    for (int q = 0; q < R; ++q) {
+      const int cta = t * R + q;
+      const uint32_t* p = part + (size_t)cta * (size_t)tile_w;
+      if (__ldg(fmt + cta) == 0u) {
+        const uint4 x = __ldcs(reinterpret_cast<const uint4*>(p + (c8 >> 1)));
+        s[0] += x.x & 0xFFFFu;
+        s[1] += x.x >> 16;
+        s[2] += x.y & 0xFFFFu;
+        s[3] += x.y >> 16;
+        s[4] += x.z & 0xFFFFu;
+        s[5] += x.z >> 16;
+        s[6] += x.w & 0xFFFFu;
+        s[7] += x.w >> 16;
+      } else {
+        const uint4 x0 = __ldcs(reinterpret_cast<const uint4*>(p + c8));
+        const uint4 x1 = __ldcs(reinterpret_cast<const uint4*>(p + c8 + 4));
+        s[0] += x0.x;
+        s[1] += x0.y;
+        s[2] += x0.z;
+        s[3] += x0.w;
+        s[4] += x1.x;
+        s[5] += x1.y;
+        s[6] += x1.z;
+        s[7] += x1.w;
+      }
+    }
+    float o[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) o[j] = (float)s[j] * w;
+    if (vec_out && gc + 7 < n) {
+      *reinterpret_cast<float4*>(out + gc) = make_float4(o[0], o[1], o[2], o[3]);
+      *reinterpret_cast<float4*>(out + gc + 4) = make_float4(o[4], o[5], o[6], o[7]);
+    } else {
+      for (int j = 0; j < 8; ++j)
+        if (gc + j < n) out[gc + j] = o[j];
+    }
+  }
+}
+
 static int max_smem_optin() {
   static int cache[64] = {0};
   int dev = 0;
@@ -737,6 +1085,41 @@ static bp_status tiled_args_from_plan(const bp_csr_plan* plan, int cluster, Tile
   return BP_OK;
 }
 
+// A plan whose tile of 32-bit counts does not fit one CTA's shared memory runs the split path
+// (16-bit counters, partial counts in the workspace); only homogeneous plans are built that way.
+static bool is_split_plan(const bp_csr_plan* plan) {
+  return plan->heter == 0 && plan->tile_w % 64 == 0 && plan->tile_w <= kSplitMaxTile &&
+         tiled_smem_bytes(acc_words_for(plan->tile_w, 1)) > (size_t)max_smem_optin() - kStaticSmemReserve;
+}
+
+// CTAs per tile of the split path: the tiles share the device's SMs, one CTA each
+static int split_count(const bp_csr_plan* plan) {
+  const int64_t nb = (plan->m + kCompactRows - 1) / kCompactRows;
+  int64_t R = device_sm_count() / std::max<int64_t>(plan->n_tiles, 1);
+  R = std::min<int64_t>(R, std::min<int64_t>(nb, kSplitMaxSplits));
+  return (int)std::max<int64_t>(R, 1);
+}
+
+struct SplitLayout {
+  size_t off_counts, off_fmt, off_part, total;
+};
+
+static SplitLayout split_layout(const bp_csr_plan* plan) {
+  const int64_t nb = (plan->m + kCompactRows - 1) / kCompactRows;
+  const int64_t ctas = (int64_t)plan->n_tiles * split_count(plan);
+  SplitLayout L;
+  L.off_counts = align_up(sizeof(int32_t) * (size_t)nb * kCompactRows, 256);
+  L.off_fmt = L.off_counts + align_up(sizeof(int32_t) * (size_t)nb, 256);
+  L.off_part = L.off_fmt + align_up(sizeof(uint32_t) * (size_t)ctas, 256);
+  L.total = L.off_part + sizeof(uint32_t) * (size_t)ctas * (size_t)plan->tile_w;
+  return L;
+}
+
+static size_t split_smem_bytes(int tile_w) { return sizeof(uint32_t) * (size_t)(tile_w / 2) + sizeof(int) * (kBlockGroup + 1); }
+
+static bp_status split_call(const bp_csr_plan* plan, const float* w_homo, const void* events, bp_etype etype,
+                            float* out, void* workspace, cudaStream_t st);
+
 }  // namespace bp
 
 using namespace bp;
@@ -809,20 +1192,31 @@ bp_status bp_csr_plan_build(const float* data, int64_t ndata, const void* indice
   uint32_t* so = reinterpret_cast<uint32_t*>(base + L.off_seg);
   uint16_t* idx = reinterpret_cast<uint16_t*>(base + L.off_idx);
   float* w = heter ? reinterpret_cast<float*>(base + L.off_w) : nullptr;
+  uint32_t* meta = reinterpret_cast<uint32_t*>(base + L.off_meta);
+  // meta[0] nonzero: no repeated column seen yet; meta[1] = 0: longest row so far (memsets, so
+  // that a plan built inside a stream capture stays capturable)
+  BP_CUDA_TRY(cudaMemsetAsync(meta, 1, sizeof(uint32_t), st));
+  BP_CUDA_TRY(cudaMemsetAsync(meta + 1, 0, sizeof(uint32_t), st));
   if (m > 0) {
     if (nnz == 0) {
       BP_CUDA_TRY(cudaMemsetAsync(so, 0, sizeof(uint32_t) * (size_t)m * (size_t)(nt + 1), st));
     } else {
-      int grid = (int)std::min<int64_t>(m, (int64_t)device_sm_count() * 16);
-      size_t smem = sizeof(uint32_t) * (size_t)(3 * nt + 1);
+      int grid = (int)std::min<int64_t>(m, (int64_t)device_sm_count() * 8);
+      size_t smem = sizeof(uint32_t) * ((size_t)(3 * nt + 1) + 2 * kPlanDupCheckMax);
+      if (smem > 48 * 1024) {
+        BP_CUDA_TRY(cudaFuncSetAttribute(plan_build_kernel<int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem));
+        BP_CUDA_TRY(cudaFuncSetAttribute(plan_build_kernel<int64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem));
+      }
       if (itype == BP_I32)
         plan_build_kernel<int32_t><<<grid, 256, smem, st>>>(static_cast<const int32_t*>(indptr),
                                                              static_cast<const int32_t*>(indices), data, nnz, m, n,
-                                                             tile_w, (int)nt, so, idx, w);
+                                                             tile_w, (int)nt, so, idx, w, meta);
       else
         plan_build_kernel<int64_t><<<grid, 256, smem, st>>>(static_cast<const int64_t*>(indptr),
                                                              static_cast<const int64_t*>(indices), data, nnz, m, n,
-                                                             tile_w, (int)nt, so, idx, w);
+                                                             tile_w, (int)nt, so, idx, w, meta);
       bp_status s = check_launch("plan_build_kernel");
       if (s != BP_OK) return s;
     }
@@ -844,6 +1238,7 @@ bp_status bp_csr_plan_arrays(const bp_csr_plan* plan, const uint32_t** seg_off, 
 
 size_t bp_event_csrmv_planned_batch_workspace_size(const bp_csr_plan* plan, int32_t batch) {
   if (!plan || plan->m <= 0 || batch <= 0) return 256;
+  if (batch == 1 && is_split_plan(plan)) return split_layout(plan).total;
   const int64_t nb = (plan->m + kCompactRows - 1) / kCompactRows;
   return align_up(sizeof(int32_t) * (size_t)batch * (size_t)nb * kCompactRows, 256) +
          align_up(sizeof(int32_t) * (size_t)batch * (size_t)nb, 256);
@@ -881,6 +1276,12 @@ static bp_status planned_batch(const char* who, const bp_csr_plan* plan, const f
   BP_REQUIRE(!homo || w_homo != nullptr, BP_EINVAL, "%s: homogeneous plan needs w_homo", who);
   const size_t need = bp_event_csrmv_planned_batch_workspace_size(plan, batch);
   BP_REQUIRE(workspace && workspace_bytes >= need, BP_ENOMEM, "%s: workspace %zu < %zu", who, workspace_bytes, need);
+  if (is_split_plan(plan)) {
+    BP_REQUIRE(!dense && batch == 1, BP_ENOTSUP,
+               "%s: a plan of %d-column tiles (16-bit counters) serves one event vector a call; build a plan "
+               "with a smaller tile (bp_csr_plan_default_tile) for dense vectors and batches", who, plan->tile_w);
+    return split_call(plan, w_homo, vec, etype, out, workspace, st);
+  }
   TiledArgs a;
   double chunks = 0.0;
   bp_status s = tiled_args_from_plan(plan, cluster, a, chunks, who);
@@ -903,6 +1304,77 @@ static bp_status planned_batch(const char* who, const bp_csr_plan* plan, const f
 }
 
 }  // namespace bp
+
+namespace bp {
+
+static bp_status split_call(const bp_csr_plan* plan, const float* w_homo, const void* events, bp_etype etype,
+                            float* out, void* workspace, cudaStream_t st) {
+  PlanView v = plan_view(plan);
+  const SplitLayout L = split_layout(plan);
+  char* ws = static_cast<char*>(workspace);
+  SplitArgs a;
+  a.seg_off = v.seg_off;
+  a.idx = v.idx;
+  a.meta = v.meta;
+  a.lists = reinterpret_cast<const int32_t*>(ws);
+  a.counts = reinterpret_cast<const int32_t*>(ws + L.off_counts);
+  a.fmt = reinterpret_cast<uint32_t*>(ws + L.off_fmt);
+  a.part = reinterpret_cast<uint32_t*>(ws + L.off_part);
+  a.m = plan->m;
+  a.n = plan->n;
+  a.tile_w = plan->tile_w;
+  a.n_tiles = plan->n_tiles;
+  a.nb = (int)((plan->m + kCompactRows - 1) / kCompactRows);
+  a.R = split_count(plan);
+  ScopedKernelTimer tk(st);  // brackets the call's three kernels
+  bp_status s = compact_blocked(events, etype, plan->m, 1, reinterpret_cast<int32_t*>(ws),
+                                reinterpret_cast<int32_t*>(ws + L.off_counts), st);
+  if (s != BP_OK) return s;
+  static bool done[64] = {false};
+  BP_CUDA_TRY(prepare_kernel(ecsr_t_split_kernel, done));
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(a.n_tiles * a.R), 1, 1);
+  cfg.blockDim = dim3(kTiledThreads, 1, 1);
+  cfg.dynamicSmemBytes = split_smem_bytes(a.tile_w);
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  BP_CUDA_TRY(cudaLaunchKernelEx(&cfg, ecsr_t_split_kernel, a));
+  const int64_t groups = (int64_t)a.n_tiles * (a.tile_w >> 3);
+  cudaLaunchConfig_t rcfg = {};
+  rcfg.gridDim = dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>((groups + 255) / 256, (int64_t)device_sm_count() * 8)), 1, 1);
+  rcfg.blockDim = dim3(256, 1, 1);
+  rcfg.stream = st;
+  rcfg.attrs = attr;
+  rcfg.numAttrs = 1;
+  const int32_t vec_out = (reinterpret_cast<uintptr_t>(out) & 15u) == 0 ? 1 : 0;
+  BP_CUDA_TRY(cudaLaunchKernelEx(&rcfg, split_reduce_kernel, (const uint32_t*)a.part, (const uint32_t*)a.fmt, w_homo,
+                                 out, (int64_t)a.n, (int32_t)a.tile_w, (int32_t)a.n_tiles, (int32_t)a.R, vec_out));
+  return BP_OK;
+}
+
+}  // namespace bp
+
+extern "C" {
+
+int32_t bp_csr_plan_count_tile(int64_t n) {
+  // the split path pays off once a call reads few enough, large enough segments: at least
+  // 2^19 columns, tiles of at most kSplitMaxTile columns that still exceed one CTA's 32-bit
+  // accumulator
+  if (n < (1 << 19)) return 0;
+  const int64_t nt = (n + kSplitMaxTile - 1) / kSplitMaxTile;
+  int64_t tw = (n + nt - 1) / nt;
+  tw = (tw + 63) / 64 * 64;
+  if (tw > kSplitMaxTile) tw = kSplitMaxTile;
+  const int64_t cap = ((int64_t)max_smem_optin() - (int64_t)kStaticSmemReserve - 4 * (kBlockGroup + 1)) / 4;
+  if (tw <= cap) return 0;
+  return (int32_t)tw;
+}
+
+}  // extern "C"
 
 extern "C" {
 

@@ -15,6 +15,9 @@
 //                               [seg_off[r][t], seg_off[r][t+1]) of idx (8 entries each)
 //   idx[entries]        uint16
 //   w[entries]          float32 (heterogeneous plans only)
+//   meta[2]             uint32  meta[0] != 0 when no row holds a column twice (checked for rows of
+//                               up to kPlanDupCheckMax entries, longer rows count as not checked
+//                               and clear it); meta[1] = the longest row's length
 // Row r's chunks start at entry align8(indptr[r]) + (8*T + 8) * r, a bound that needs no
 // prefix sum (row r needs at most nnz_r + 7*T padded entries and the gap to row r + 1 is at
 // least nnz_r + 8*T + 1).  Chunk indices are 32-bit: a plan holds fewer than 2^32 chunks.
@@ -27,10 +30,11 @@ namespace bp {
 constexpr int kPlanMaxTiles = 4000;  // plan build keeps 3 x n_tiles words in 48 KB of shared memory
 constexpr int kPlanMaxTileW = 65535;  // local indices and the pad value tile_w are uint16
 constexpr int kChunkEntries = 8;      // entries per 16-byte chunk
+constexpr int kPlanDupCheckMax = 4096;  // rows up to this length are checked for repeated columns
 
 // Byte offsets of the arrays inside the plan memory.
 struct PlanLayout {
-  size_t off_seg, off_idx, off_w, total;
+  size_t off_seg, off_idx, off_w, off_meta, total;
   uint64_t entries, chunks;
 };
 
@@ -42,7 +46,8 @@ inline PlanLayout plan_layout(int64_t m, int64_t nnz, int32_t n_tiles, bool hete
   L.off_seg = 0;
   L.off_idx = align_up(sizeof(uint32_t) * (size_t)m * (size_t)(n_tiles + 1), 256);
   L.off_w = L.off_idx + align_up(sizeof(uint16_t) * (size_t)L.entries, 256);
-  L.total = L.off_w + (heter ? align_up(sizeof(float) * (size_t)L.entries, 256) : 0);
+  L.off_meta = L.off_w + (heter ? align_up(sizeof(float) * (size_t)L.entries, 256) : 0);
+  L.total = L.off_meta + 256;
   return L;
 }
 
@@ -50,6 +55,7 @@ struct PlanView {
   const uint32_t* seg_off;
   const uint16_t* idx;
   const float* w;
+  const uint32_t* meta;
   int64_t m, n;
   int32_t tile_w, n_tiles;
 };
@@ -61,6 +67,7 @@ inline PlanView plan_view(const bp_csr_plan* p) {
   v.seg_off = reinterpret_cast<const uint32_t*>(base + L.off_seg);
   v.idx = reinterpret_cast<const uint16_t*>(base + L.off_idx);
   v.w = p->heter ? reinterpret_cast<const float*>(base + L.off_w) : nullptr;
+  v.meta = reinterpret_cast<const uint32_t*>(base + L.off_meta);
   v.m = p->m;
   v.n = p->n;
   v.tile_w = p->tile_w;

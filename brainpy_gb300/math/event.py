@@ -17,7 +17,8 @@ from .. import tuning
 from . import _grad
 from ._utils import as_tensor, default_device, event_type, float_data, index_type
 
-__all__ = ["csrmv", "csrmv_taichi", "csrmv_batch", "info", "CSRPlan", "prepare", "autotune"]
+__all__ = ["csrmv", "csrmv_taichi", "csrmv_batch", "info", "CSRPlan", "prepare", "autotune", "release_plans",
+           "plan_cache_bytes"]
 
 
 class CSRPlan:
@@ -29,17 +30,26 @@ class CSRPlan:
   own device memory; it is a function of the arrays at build time.
   """
 
-  def __init__(self, indices, indptr, shape, data=None, tile_w=None, cluster=4):
+  def __init__(self, indices, indptr, shape, data=None, tile_w=None, cluster=4, kind="general"):
     dev = indices.device
     self.shape = (int(shape[0]), int(shape[1]))
     self.cluster = int(cluster)
     m, n = self.shape
     L = _lib.lib()
     heter = data is not None and data.numel() > 1
+    if kind not in ("general", "count"):
+      raise ValueError(f"plan kind must be 'general' or 'count', got {kind!r}")
+    # "count": tiles of up to 65,472 columns with 16-bit counters and per-tile partial counts
+    # (event products with a homogeneous weight, one vector a call); "general": tiles whose
+    # 32-bit accumulator fits one CTA (every product, batches, weights)
+    if kind == "count" and tile_w is None and not heter:
+      tile_w = L.bp_csr_plan_count_tile(n) or None
     if tile_w is None:
+      kind = "general"
       tile_w = L.bp_csr_plan_default_tile(n, self.cluster)
       if tile_w <= 0:
         raise _lib.BPError("bp_csr_plan_default_tile failed: " + L.bp_last_error().decode())
+    self.kind = kind
     self.tile_w = int(tile_w)
     nbytes = L.bp_csr_plan_bytes(m, n, indices.numel(), int(heter), self.tile_w)
     self.mem = torch.empty(max(nbytes, 1), dtype=torch.uint8, device=dev)
@@ -221,50 +231,95 @@ def prepare(indices, indptr, *, shape, data=None, tile_w=None, cluster=4) -> CSR
 
 
 # ---- automatic plan cache ---------------------------------------------------------
-# Keyed by the identity and version counter of the CSR tensors (and of heterogeneous
-# weights), so an in-place change of any of them invalidates the entry.  _ROUTES holds, under
-# the same keys, the kernel family `autotune` chose for a matrix ("row" or "tiled"); a matrix
-# without a route takes the tiled plan from the size thresholds below.
-_PLANS = {}
-_ROUTES = {}
+# Keyed by the identity of the CSR tensors (and of heterogeneous weights) and the plan kind.
+# Every entry remembers the tensors' version counters: an in-place change of any of them
+# (STDP updates of the weights, for instance) replaces the entry, so the stale plan's memory
+# is released at once instead of staying beside the new one.  _ROUTES holds, under the
+# matrix key, the kernel family `autotune` chose ("row", "tiled" or "split"); a matrix without
+# a route takes a plan from the size thresholds below.  `release_plans()` drops everything.
+_PLANS = {}   # (matrix key, kind) -> (weak refs, versions, CSRPlan)
+_ROUTES = {}  # matrix key -> (weak refs, versions, route)
 _PLAN_MIN_N = int(os.environ.get("BPGPU_PLAN_MIN_N", 1 << 15))
 _PLAN_MIN_NNZ = int(os.environ.get("BPGPU_PLAN_MIN_NNZ", 1 << 20))
 _PLAN_DISABLE = os.environ.get("BPGPU_DISABLE_PLAN", "0") == "1"
+# homogeneous event products on at least this many columns take the split plan (tiles of up
+# to 65,472 columns, 16-bit counters): half the segment reads of the general plan
+_SPLIT_MIN_N = int(os.environ.get("BPGPU_SPLIT_MIN_N", 1 << 19))
 
 
-def _plan_key(t):
-  return (id(t), t.data_ptr(), t._version)
+def _ident(t):
+  return (id(t), t.data_ptr())
 
 
 def _matrix_key(data, indices, indptr, m, n):
   heter = data.numel() > 1
-  return (_plan_key(indices), _plan_key(indptr), int(m), int(n), _plan_key(data) if heter else None)
+  return (_ident(indices), _ident(indptr), int(m), int(n), _ident(data) if heter else None)
+
+
+def _versions(data, indices, indptr):
+  return (indices._version, indptr._version, data._version if data.numel() > 1 else None)
 
 
 def _matrix_refs(data, indices, indptr):
   return [weakref.ref(indices), weakref.ref(indptr)] + ([weakref.ref(data)] if data.numel() > 1 else [])
 
 
+def _alive(refs):
+  return all(r() is not None for r in refs)
+
+
+def _set_route(data, indices, indptr, shape, route):
+  """Records the kernel family of this matrix ("row", "tiled" or "split"); returns its key."""
+  key = _matrix_key(data, indices, indptr, shape[0], shape[1])
+  _ROUTES[key] = (_matrix_refs(data, indices, indptr), _versions(data, indices, indptr), route)
+  return key
+
+
 def _route(data, indices, indptr, shape):
-  """The autotuned kernel family of this matrix: "row", "tiled", or None (not tuned)."""
+  """The autotuned kernel family of this matrix: "row", "tiled", "split", or None (not tuned,
+  or the arrays changed since)."""
   if not _ROUTES:
     return None
   key = _matrix_key(data, indices, indptr, shape[0], shape[1])
   ent = _ROUTES.get(key)
   if ent is None:
     return None
-  refs, route = ent
-  if all(r() is not None for r in refs):
+  refs, ver, route = ent
+  if _alive(refs) and ver == _versions(data, indices, indptr):
     return route
   del _ROUTES[key]
   return None
 
 
-def _cached_plan(data, indices, indptr, shape, force=False, routed=True):
+def _plan_kind(data, n, route):
+  """Plan kind of an event product: "count" (split plan) for a homogeneous weight on many
+  columns, unless the autotuner chose the general plan; "general" otherwise."""
+  if data.numel() > 1 or route == "tiled":
+    return "general"
+  if route == "split":
+    return "count"
+  return "count" if int(n) >= _SPLIT_MIN_N else "general"
+
+
+def release_plans():
+  """Drops every cached plan and autotuned route.  Their device memory is freed once no other
+  reference holds the plans (a plan of a 1e6 x 1e6 matrix with fan-out 1000 is about 2.6 GB)."""
+  _PLANS.clear()
+  _ROUTES.clear()
+
+
+def plan_cache_bytes():
+  """Device bytes held by the cached plans."""
+  return sum(int(p.mem.numel()) for _, _, p in _PLANS.values())
+
+
+def _cached_plan(data, indices, indptr, shape, force=False, routed=True, kind="general"):
   """The plan of this matrix (built on first use), or None when the matrix is below the
   size thresholds, plans are disabled, or the autotuner routed its event product to the row
-  kernel.  `force` builds one below the thresholds (an autotuned "tiled" route, or tuning
-  itself); `routed=False` ignores the event product's route (the dense-vector products)."""
+  kernel.  `force` builds one below the thresholds (an autotuned "tiled"/"split" route, or
+  tuning itself); `routed=False` ignores the event product's route (the dense-vector products).
+  kind "count" asks for the split plan (homogeneous weights only; other matrices get the
+  general plan)."""
   if _PLAN_DISABLE:
     return None
   m, n = int(shape[0]), int(shape[1])
@@ -275,22 +330,25 @@ def _cached_plan(data, indices, indptr, shape, force=False, routed=True):
     if route is None and (n < _PLAN_MIN_N or indices.numel() < _PLAN_MIN_NNZ):
       return None
   heter = data.numel() > 1
-  key = _matrix_key(data, indices, indptr, m, n)
+  if heter:
+    kind = "general"
+  key = (_matrix_key(data, indices, indptr, m, n), kind)
+  ver = _versions(data, indices, indptr)
   ent = _PLANS.get(key)
   if ent is not None:
-    refs, plan = ent
-    if all(r() is not None for r in refs):
+    refs, v, plan = ent
+    if _alive(refs) and v == ver:
       return plan
-    del _PLANS[key]
-  for k in [k for k, (refs, _) in _PLANS.items() if any(r() is None for r in refs)]:
+    del _PLANS[key]  # stale: release its memory before building the new plan
+  for k in [k for k, (refs, _, _) in _PLANS.items() if not _alive(refs)]:
     del _PLANS[k]
-  plan = CSRPlan(indices, indptr, (m, n), data if heter else None)
-  _PLANS[key] = (_matrix_refs(data, indices, indptr), plan)
+  plan = CSRPlan(indices, indptr, (m, n), data if heter else None, kind=kind)
+  _PLANS[key] = (_matrix_refs(data, indices, indptr), ver, plan)
   return plan
 
 
 def _valid_choice(choice):
-  if choice == "row":
+  if choice in ("row", "split"):
     return True
   if not isinstance(choice, str) or not choice.startswith("tiled:"):
     return False
@@ -351,18 +409,26 @@ def autotune(data, indices, indptr, events, *, shape: Tuple[int, int], transpose
           plan.variant = code
           return plan.csrmv(events, w, out=out, float_rule=float_rule)
         cands[f"tiled:{code}"] = run
+      if not heter and _lib.lib().bp_csr_plan_count_tile(n) > 0:
+        split = _cached_plan(d, indices, indptr, (m, n), force=True, kind="count")
+        cands["split"] = lambda: split.csrmv(events, d, out=out, float_rule=float_rule)
     best, times = tuning.pick(cands, timer or tuning.cuda_timer(reps))
     rec = {"choice": best, "times_us": times, "rate": rate}
     cache.store(key, rec)
     cache.save()
   mkey = _matrix_key(d, indices, indptr, m, n)
-  if rec["choice"] == "row" or _PLAN_DISABLE:
-    _ROUTES[mkey] = (_matrix_refs(d, indices, indptr), "row")
-    _PLANS.pop(mkey, None)  # the row kernel needs no plan: release its memory
-  else:
+  choice = rec["choice"] if not _PLAN_DISABLE else "row"
+  route = choice.split(":", 1)[0]
+  _set_route(d, indices, indptr, (m, n), route)
+  # keep only the plan the chosen family runs on: each holds about 2.6 bytes per stored entry
+  for kind in ("general", "count"):
+    if route == "row" or (route == "split") != (kind == "count"):
+      _PLANS.pop((mkey, kind), None)
+  if route == "tiled":
     plan = _cached_plan(d, indices, indptr, (m, n), force=True)
-    plan.variant = int(rec["choice"].split(":", 1)[1])
-    _ROUTES[mkey] = (_matrix_refs(d, indices, indptr), "tiled")
+    plan.variant = int(choice.split(":", 1)[1])
+  elif route == "split":
+    _cached_plan(d, indices, indptr, (m, n), force=True, kind="count")
   return rec
 
 
@@ -404,7 +470,9 @@ def _event_csrmv(data, indices, indptr, events, shape, transpose, float_rule, ou
   m, n = int(shape[0]), int(shape[1])
   n_out = n if transpose else m
   if transpose and use_plan:
-    plan = _cached_plan(data, indices, indptr, (m, n), force=_route(data, indices, indptr, (m, n)) == "tiled")
+    route = _route(data, indices, indptr, (m, n))
+    plan = _cached_plan(data, indices, indptr, (m, n), force=route in ("tiled", "split"),
+                        kind=_plan_kind(data, n, route))
     if plan is not None:
       return plan.csrmv(events, None if plan.heter else data, out=out, float_rule=float_rule)
   if out is None:
@@ -473,7 +541,7 @@ def csrmv_batch(data, indices, indptr, events, *, shape: Tuple[int, int], transp
     _check_common(d, indices, indptr, events[0], shape, True)
     if index_type(indptr, "indptr") != index_type(indices, "indices"):
       raise ValueError("indices and indptr must have the same integer type.")
-    plan = _cached_plan(d, indices, indptr, (m, n), force=_route(d, indices, indptr, (m, n)) == "tiled")
+    plan = _cached_plan(d, indices, indptr, (m, n), force=_route(d, indices, indptr, (m, n)) in ("tiled", "split"))
     if plan is not None:
       return plan.csrmv_batch(events, None if plan.heter else d, float_rule=float_rule)
   out = torch.empty((events.shape[0], n if transpose else m), dtype=torch.float32, device=dev)

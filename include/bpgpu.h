@@ -205,6 +205,17 @@ typedef struct {
 /* tile width the tiled kernels run best with on the current device for n columns and
  * clusters of `cluster` CTAs (1, 2, 4 or 8); 0 on error. */
 int32_t bp_csr_plan_default_tile(int64_t n, int32_t cluster);
+/* tile width of a counting plan for n columns, 0 when n is too small for one (n < 2^19).
+ * A counting plan has tiles of up to 65,472 columns, more than one CTA holds as 32-bit counts:
+ * bp_event_csrmv_planned runs it with 16-bit counters, R CTAs per tile (R = SMs / n_tiles, at
+ * most 16) and a second kernel that adds the R partial counts of every column (the workspace
+ * holds them).  A call then reads half as many, twice as long segments as with the default
+ * tile; DRAM serves random reads of up to ~128 bytes at a fixed rate, so the call is faster.
+ * Counting plans serve homogeneous plans and single event vectors only (BP_ENOTSUP for dense
+ * vectors and batches).  A CTA that could overflow a 16-bit count (a row holding a column
+ * twice, or more than 65,535 active rows of its share) counts in 32 bits, two passes over its
+ * rows. */
+int32_t bp_csr_plan_count_tile(int64_t n);
 size_t bp_csr_plan_bytes(int64_t m, int64_t n, int64_t nnz, int32_t heter, int32_t tile_w);
 /* The compiled tiled-kernel variants (bp_csr_plan.variant codes): writes up to `cap` codes into
  * `codes` and returns how many there are. */

@@ -103,3 +103,27 @@ def test_layer_stdp_update(bplib, orc):
   np.testing.assert_array_equal(_bits(layer.weight.cpu()), _bits(want))
   with pytest.raises(ValueError):
     dnn.EventCSRLinear((ind, ptr), 0.5, shape=(m, n)).stdp_update(on_pre={"spike": _t(pre_sp), "trace": _t(post_tr)})
+
+
+def test_stdp_loop_keeps_one_plan(bplib):
+  """In-place STDP updates bump the weights' version counter; the plan cache replaces the
+  layer's plan instead of keeping one per version, so device memory stays flat over steps."""
+  from brainpy_gb300 import dnn
+  from brainpy_gb300.connect import fixed_prob_csr
+  from brainpy_gb300.math import event as ev
+  n, k = 40_000, 40  # above the plan thresholds (n >= 32768 columns, nnz >= 2^20)
+  ind, ptr = fixed_prob_csr(n, n, k, seed=11)
+  layer = dnn.EventCSRLinear((ind, ptr), torch.full((ind.numel(),), 0.5, device="cuda"), shape=(n, n))
+  ev.release_plans()
+  rng = np.random.default_rng(12)
+  spikes = _t(rng.random(n) < 0.05)
+  trace = _t(rng.normal(0, 0.01, n).astype(np.float32))
+  mem = []
+  for _ in range(6):
+    layer.update(spikes)
+    layer.stdp_update(on_pre={"spike": spikes, "trace": trace}, w_min=0.0, w_max=1.0)
+    torch.cuda.synchronize()
+    mem.append(torch.cuda.memory_allocated())
+  assert len(ev._PLANS) == 1
+  assert mem[-1] == mem[1], mem
+  ev.release_plans()

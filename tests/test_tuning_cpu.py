@@ -88,8 +88,7 @@ def test_routes_skip_or_force_the_plan(bplib):
   indptr = torch.zeros(5, dtype=torch.int32)
   data = torch.ones(1)
   shape = (4, 1 << 20)
-  key = ev._matrix_key(data, indices, indptr, *shape)
-  ev._ROUTES[key] = (ev._matrix_refs(data, indices, indptr), "row")
+  key = ev._set_route(data, indices, indptr, shape, "row")
   try:
     assert ev._route(data, indices, indptr, shape) == "row"
     # a "row" route returns no plan, whatever the size thresholds say (nothing is built)
@@ -101,8 +100,7 @@ def test_routes_skip_or_force_the_plan(bplib):
     ev._ROUTES.pop(key, None)
   # a route whose arrays are gone is dropped on lookup
   idx2 = torch.zeros(8, dtype=torch.int32)
-  key2 = ev._matrix_key(data, idx2, indptr, *shape)
-  ev._ROUTES[key2] = (ev._matrix_refs(data, idx2, indptr), "tiled")
+  key2 = ev._set_route(data, idx2, indptr, shape, "tiled")
   del idx2
   gc.collect()
   ent = ev._ROUTES.get(key2)
@@ -113,7 +111,7 @@ def test_routes_skip_or_force_the_plan(bplib):
 def test_valid_choices(bplib):
   from brainpy_gb300.math import event as ev
   codes = ev.CSRPlan.variants()
-  assert codes and ev._valid_choice("row")
+  assert codes and ev._valid_choice("row") and ev._valid_choice("split")
   assert all(ev._valid_choice(f"tiled:{c}") for c in codes)
   for bad in ("tiled:999999", "tiled:x", "columns", None, 3):
     assert not ev._valid_choice(bad)

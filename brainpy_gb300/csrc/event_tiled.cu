@@ -533,6 +533,14 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
 constexpr int kSplitMaxTile = 65472;  // a multiple of 64 below the uint16 range
 constexpr int kSplitMaxSplits = 16;
 constexpr int kSplitRounds = 2;       // rounds of loads in flight
+constexpr int kFlatRows = 4096;       // rows a CTA-wide pass tabulates
+constexpr int kFlatRounds = 1024;     // rounds of 32 chunks a pass holds (32,768 chunks)
+
+// shared memory of the split kernel: accumulator, block offsets, the CTA-wide pass tables
+static size_t split_smem_bytes(int tile_w) {
+  return sizeof(uint32_t) * (size_t)(tile_w / 2) + sizeof(int) * (kBlockGroup + 1) +
+         sizeof(uint32_t) * (size_t)(2 * kFlatRows + kFlatRows / 32 + 2 * kFlatRounds);
+}
 
 struct SplitArgs {
   const uint32_t* seg_off;
@@ -553,7 +561,17 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const Sp
   const uint32_t acc_s = (uint32_t)__cvta_generic_to_shared(acc);
   const int half_w = a.tile_w >> 1;  // words of the accumulator: 16-bit pairs, or one half in 32 bits
   int* s_boff = reinterpret_cast<int*>(smem + sizeof(uint32_t) * (size_t)half_w);  // kBlockGroup + 1
+  // CTA-wide pass tables: segment start chunk and exclusive chunk prefix of each tabulated row,
+  // empty-segment bits, and per round of 32 chunks the bitmask of segment starts in it and the
+  // segment owning its first chunk
+  uint32_t* t_st = reinterpret_cast<uint32_t*>(s_boff + kBlockGroup + 1);
+  uint32_t* t_P = t_st + kFlatRows;
+  uint32_t* t_emp = t_P + kFlatRows;
+  uint32_t* t_M = t_emp + kFlatRows / 32;
+  uint32_t* t_first = t_M + kFlatRounds;
   __shared__ int s_wsum[32];
+  __shared__ int s_cut;
+  __shared__ uint32_t s_tot;
   const int tile = blockIdx.x / a.R, q = blockIdx.x % a.R;
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
@@ -742,8 +760,143 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const Sp
     }
   };
 
+  // CTA-wide flat passes (16-bit counters, one group of blocks): up to kFlatRows rows and
+  // kFlatRounds * 32 chunks a pass.  Rounds go to warps round-robin, so the warps stay within
+  // a round of each other whatever the segment lengths.
+  auto run_flat = [&]() {
+    const int ng = b1 - b0;
+    const uint32_t lane_le1 = (lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u)) & ~1u;
+    for (int i0 = 0; i0 < rows;) {
+      const int cnt = min(kFlatRows, rows - i0);
+      __syncthreads();  // the previous pass's tables are no longer read
+      for (int i = tid; i < kFlatRows / 32; i += nthr) t_emp[i] = 0u;
+      if (tid == 0) s_cut = cnt;
+      __syncthreads();
+      // segment bounds of rows i0 .. i0 + cnt (four rows a thread, loads issued together)
+      {
+        uint32_t st[4], en[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int i = tid + k * nthr;
+          st[k] = en[k] = 0u;
+          if (i < cnt) {
+            const int j = i0 + i;
+            int l = 0, h = ng;
+            while (h - l > 1) {
+              const int mid = (l + h) >> 1;
+              if (s_boff[mid] <= j) l = mid;
+              else h = mid;
+            }
+            const int32_t row = __ldg(a.lists + (int64_t)(b0 + l) * kCompactRows + (j - s_boff[l]));
+            const uint32_t* so = a.seg_off + (int64_t)row * so_stride + tile;
+            st[k] = __ldg(so);
+            en[k] = __ldg(so + 1);
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int i = tid + k * nthr;
+          if (i < cnt) {
+            t_st[i] = st[k];
+            t_P[i] = max(en[k] - st[k], 1u);  // an empty segment takes one chunk, skipped
+            if (en[k] == st[k]) atomicOr(&t_emp[i >> 5], 1u << (i & 31));
+          }
+        }
+      }
+      __syncthreads();
+      // exclusive prefix of the chunk counts, four consecutive rows a thread
+      {
+        uint32_t c[4], loc = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int i = 4 * tid + k;
+          c[k] = i < cnt ? t_P[i] : 0u;
+          loc += c[k];
+        }
+        uint32_t incl = loc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t t = __shfl_up_sync(FULL, incl, o);
+          if (lane >= o) incl += t;
+        }
+        if (lane == 31) s_wsum[warp] = (int)incl;
+        __syncthreads();
+        if (warp == 0) {
+          const int t = lane < nwarps ? s_wsum[lane] : 0;
+          int ti = t;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(FULL, ti, o);
+            if (lane >= o) ti += u;
+          }
+          s_wsum[lane] = ti - t;
+        }
+        __syncthreads();
+        uint32_t run = (uint32_t)s_wsum[warp] + incl - loc;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int i = 4 * tid + k;
+          if (i < cnt) {
+            t_P[i] = run;
+            run += c[k];
+            if (run > (uint32_t)(32 * kFlatRounds)) atomicMin(&s_cut, i);  // row i ends past the pass's rounds
+            if (i == cnt - 1) s_tot = run;
+          }
+        }
+      }
+      __syncthreads();
+      // a dup-free row fits a pass (its segment has at most tile_w / 8 + 1 chunks), so a pass
+      // takes at least one row
+      const int cut = max(s_cut, 1);
+      const uint32_t Ctot = cut < cnt ? t_P[cut] : s_tot;
+      // at most kFlatRounds: a pass ends before the row that would pass it, and a first row
+      // alone fits (see above); the clamp keeps the tables in bounds whatever the input
+      const int nr = min((int)((Ctot + 31u) >> 5), kFlatRounds);
+      for (int r = tid; r < nr; r += nthr) t_M[r] = 0u;
+      __syncthreads();
+      for (int i = tid; i < cut; i += nthr) {
+        const uint32_t p = t_P[i], e = (i + 1 < cut) ? t_P[i + 1] : Ctot;
+        atomicOr(&t_M[p >> 5], 1u << (p & 31u));
+        for (uint32_t r = (p + 31u) >> 5; (r << 5) < e && r < (uint32_t)nr; ++r) t_first[r] = (uint32_t)i;
+      }
+      __syncthreads();
+      // rounds r = warp, warp + W, ...: lane l takes chunk 32 r + l; its owner is the segment of
+      // the round's first chunk plus the segment starts at positions 1 .. l of the round
+      auto round_load = [&](int r, uint4& v, uint32_t& lim) {
+        v = make_uint4(0u, 0u, 0u, 0u);
+        lim = 0u;
+        if (r >= nr) return;
+        const uint32_t g = ((uint32_t)r << 5) + lane;
+        if (g < Ctot) {
+          const uint32_t o = min(t_first[r] + __popc(t_M[r] & lane_le1), (uint32_t)cut - 1u);
+          lim = ((t_emp[o >> 5] >> (o & 31u)) & 1u) ? 0u : tile_w;
+          v = ld_stream_u4(a.idx + 8ull * (t_st[o] + (g - t_P[o])));
+        }
+      };
+      uint4 v0, v1, v2;
+      uint32_t l0, l1, l2;
+      int r = warp;
+      round_load(r, v0, l0);
+      round_load(r + nwarps, v1, l1);
+      for (; r < nr; r += nwarps) {
+        round_load(r + 2 * nwarps, v2, l2);
+        const uint32_t x[8] = {v0.x & 0xFFFFu, v0.x >> 16, v0.y & 0xFFFFu, v0.y >> 16,
+                               v0.z & 0xFFFFu, v0.z >> 16, v0.w & 0xFFFFu, v0.w >> 16};
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          red_if(x[e], l0, acc_s + ((x[e] >> 1) << 2), (x[e] & 1u) ? 0x10000u : 1u);
+        v0 = v1;
+        l0 = l1;
+        v1 = v2;
+        l1 = l2;
+      }
+      i0 += cut;
+    }
+  };
+
   if (packed) {
-    run_split(std::true_type{}, 0u);
+    if (one_group) run_flat();
+    else run_split(std::true_type{}, 0u);
     __syncthreads();
     const uint4* acc4 = reinterpret_cast<const uint4*>(acc);
     uint4* p4 = reinterpret_cast<uint4*>(part);
@@ -784,10 +937,26 @@ __global__ void __launch_bounds__(256) split_reduce_kernel(const uint32_t* __res
     const int64_t gc = (int64_t)t * tile_w + c8;
     if (gc >= n) continue;
     uint32_t s[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
-    for (int q = 0; q < R; ++q) {
+    uint32_t wide = 0u;  // bit q: split q of this tile wrote 32-bit counts
+    for (int q = 0; q < R; ++q) wide |= (__ldg(fmt + t * R + q) != 0u ? 1u : 0u) << q;
+    if (wide == 0u) {
+      // every split wrote 16-bit pairs: loads of four splits in flight at a time
+#pragma unroll 4
+      for (int q = 0; q < R; ++q) {
+        const uint4 x = __ldcs(reinterpret_cast<const uint4*>(part + (size_t)(t * R + q) * (size_t)tile_w + (c8 >> 1)));
+        s[0] += x.x & 0xFFFFu;
+        s[1] += x.x >> 16;
+        s[2] += x.y & 0xFFFFu;
+        s[3] += x.y >> 16;
+        s[4] += x.z & 0xFFFFu;
+        s[5] += x.z >> 16;
+        s[6] += x.w & 0xFFFFu;
+        s[7] += x.w >> 16;
+      }
+    } else for (int q = 0; q < R; ++q) {
       const int cta = t * R + q;
       const uint32_t* p = part + (size_t)cta * (size_t)tile_w;
-      if (__ldg(fmt + cta) == 0u) {
+      if (((wide >> q) & 1u) == 0u) {
         const uint4 x = __ldcs(reinterpret_cast<const uint4*>(p + (c8 >> 1)));
         s[0] += x.x & 0xFFFFu;
         s[1] += x.x >> 16;
@@ -1114,8 +1283,6 @@ static SplitLayout split_layout(const bp_csr_plan* plan) {
   L.total = L.off_part + sizeof(uint32_t) * (size_t)ctas * (size_t)plan->tile_w;
   return L;
 }
-
-static size_t split_smem_bytes(int tile_w) { return sizeof(uint32_t) * (size_t)(tile_w / 2) + sizeof(int) * (kBlockGroup + 1); }
 
 static bp_status split_call(const bp_csr_plan* plan, const float* w_homo, const void* events, bp_etype etype,
                             float* out, void* workspace, cudaStream_t st);

@@ -92,7 +92,7 @@ class CsrPlan(ctypes.Structure):
   """Mirror of bp_csr_plan (include/bpgpu.h)."""
   _fields_ = [("m", _c_i64), ("n", _c_i64), ("nnz", _c_i64), ("tile_w", _c_i32), ("n_tiles", _c_i32),
               ("heter", _c_i32), ("variant", _c_i32), ("entries", ctypes.c_uint64), ("mem", _c_ptr),
-              ("bytes", _c_size)]
+              ("bytes", _c_size), ("kind", _c_i32)]
 
 
 class LifParams(ctypes.Structure):

@@ -512,34 +512,31 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
 }
 
 // ---------------------------------------------------------------------------
-// split accumulation for large column tiles (homogeneous weight, events)
+// split accumulation: counting plans (homogeneous weight, events)
 // ---------------------------------------------------------------------------
 // DRAM serves random reads of up to ~128 bytes at a fixed rate of row activations, so the
-// number of segment reads a call makes sets its floor.  Tiles of up to 65,472 columns halve
-// that number against the cluster path's ~28K-column tiles (a row's segment for a tile is
-// ~125 bytes at fan-out 1000 and 16 tiles), but such a tile fits shared memory only as 16-bit
-// counters (two columns per 32-bit word, 125 KB).  CTA (tile t, split q) accumulates the
-// active rows of compaction blocks [q nb / R, (q + 1) nb / R) and writes its counts to the
-// workspace; split_reduce_kernel then adds the R partial counts of every column and writes
-// (float)count * w.
-//   - 16-bit counters are exact while no column gets 65,536 adds from one CTA: the plan has no
-//     repeated column in any row (plan meta[0]) and the CTA sees at most 65,535 active rows.
-//     Otherwise the CTA runs two passes over its rows with 32-bit counters, one for each half
-//     of the tile, and marks its partial as 32-bit.
-//   - The loop distributes a slice's chunks flat over the warp (chunk 32j + l of the slice's
-//     segments to lane l in round j), so every round but a slice's last keeps all lanes busy
-//     whatever the segment lengths; the loads of the next rounds are in flight while a round's
-//     shared-memory adds issue.
-constexpr int kSplitMaxTile = 65472;  // a multiple of 64 below the uint16 range
+// number of segment reads sets a call's floor.  A counting plan's tiles are as wide as a
+// CTA's shared memory holds 32-bit counts (~50K columns, 20 tiles at N = 1e6, against the
+// cluster path's ~28K columns), so a call reads fewer, longer segments.  CTA (tile t, split q)
+// counts the active rows of compaction blocks [q nb / R, (q + 1) nb / R) for its tile and
+// writes them to the workspace; split_reduce_kernel adds the R partial counts of a column and
+// writes (float)count * w.
+//   - Counting: one shared-memory add of 1 per entry, unpredicated.  The pad index tile_w and
+//     every entry of an inactive lane or an empty segment add to a dummy word past the tile.
+//   - Work: the CTA tabulates its rows' segments in shared memory (start chunk, chunk prefix)
+//     and deals the flattened chunks out in rounds of 32, round r to warp r mod W, chunk
+//     32 r + l to lane l; the warps stay within a round of each other whatever the segment
+//     lengths, and the loads of the next rounds are in flight while a round's adds issue.
+//   - Partial counts are written as 16-bit pairs when no column can reach 65,536 in one CTA
+//     (no repeated column in any row, at most 65,535 active rows), as 32-bit counts otherwise.
+constexpr int kFlatRows = 2048;    // rows a CTA-wide pass tabulates
+constexpr int kFlatRounds = 1024;  // rounds of 32 chunks a pass holds (32,768 chunks)
 constexpr int kSplitMaxSplits = 16;
-constexpr int kSplitRounds = 2;       // rounds of loads in flight
-constexpr int kFlatRows = 4096;       // rows a CTA-wide pass tabulates
-constexpr int kFlatRounds = 1024;     // rounds of 32 chunks a pass holds (32,768 chunks)
+constexpr int kSplitDummy = 32;    // words past the tile: the pad index tile_w lands in the first
 
-// shared memory of the split kernel: accumulator, block offsets, the CTA-wide pass tables
+static size_t split_table_bytes() { return sizeof(uint32_t) * (size_t)(2 * kFlatRows + kFlatRows / 32 + 2 * kFlatRounds); }
 static size_t split_smem_bytes(int tile_w) {
-  return sizeof(uint32_t) * (size_t)(tile_w / 2) + sizeof(int) * (kBlockGroup + 1) +
-         sizeof(uint32_t) * (size_t)(2 * kFlatRows + kFlatRows / 32 + 2 * kFlatRounds);
+  return sizeof(uint32_t) * (size_t)(tile_w + kSplitDummy) + sizeof(int) * (kBlockGroup + 1) + split_table_bytes();
 }
 
 struct SplitArgs {
@@ -554,16 +551,17 @@ struct SplitArgs {
   int32_t tile_w, n_tiles, nb, R;
 };
 
+__device__ __forceinline__ void red1(uint32_t addr) { asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(addr)); }
+
 __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const SplitArgs a) {
   constexpr unsigned FULL = 0xffffffffu;
   extern __shared__ __align__(16) unsigned char smem[];
+  const int acc_words = a.tile_w + kSplitDummy;  // a multiple of 32
   uint32_t* acc = reinterpret_cast<uint32_t*>(smem);
   const uint32_t acc_s = (uint32_t)__cvta_generic_to_shared(acc);
-  const int half_w = a.tile_w >> 1;  // words of the accumulator: 16-bit pairs, or one half in 32 bits
-  int* s_boff = reinterpret_cast<int*>(smem + sizeof(uint32_t) * (size_t)half_w);  // kBlockGroup + 1
-  // CTA-wide pass tables: segment start chunk and exclusive chunk prefix of each tabulated row,
-  // empty-segment bits, and per round of 32 chunks the bitmask of segment starts in it and the
-  // segment owning its first chunk
+  int* s_boff = reinterpret_cast<int*>(acc + acc_words);  // kBlockGroup + 1
+  // pass tables: start chunk and exclusive chunk prefix of each tabulated row, empty-segment
+  // bits, and per round the bitmask of segment starts in it and the segment of its first chunk
   uint32_t* t_st = reinterpret_cast<uint32_t*>(s_boff + kBlockGroup + 1);
   uint32_t* t_P = t_st + kFlatRows;
   uint32_t* t_emp = t_P + kFlatRows;
@@ -576,18 +574,24 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const Sp
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
   const uint32_t tile_w = (uint32_t)a.tile_w;
+  const uint32_t pad2 = tile_w | (tile_w << 16);
+  const uint4 pads = make_uint4(pad2, pad2, pad2, pad2);  // a chunk that adds only to the dummy word
   const int64_t so_stride = a.n_tiles + 1;
-
-  auto zero_acc = [&]() {
+  {
     uint4* acc4 = reinterpret_cast<uint4*>(acc);
-    for (int i = tid; i < (half_w >> 2); i += nthr) acc4[i] = make_uint4(0u, 0u, 0u, 0u);
-  };
-  zero_acc();
+    for (int i = tid; i < (acc_words >> 2); i += nthr) acc4[i] = make_uint4(0u, 0u, 0u, 0u);
+  }
   const int b0 = (int)((int64_t)q * a.nb / a.R), b1 = (int)((int64_t)(q + 1) * a.nb / a.R);
 
   // the compaction kernel of this call may still be running (programmatic dependent launch)
   cudaGridDependencySynchronize();
 
+  auto add8 = [&](const uint4 v) {
+    const uint32_t x[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
+                           v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
+#pragma unroll
+    for (int e = 0; e < 8; ++e) red1(acc_s + (x[e] << 2));
+  };
   // exclusive prefix of the active-row counts of blocks [g0, g0 + ng) into s_boff; returns the total
   auto group_prefix = [&](int g0, int ng) -> int {
     __syncthreads();  // s_boff / s_wsum of an earlier use are no longer read
@@ -615,7 +619,6 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const Sp
     __syncthreads();
     return s_boff[ng];
   };
-  // active rows of the whole split (several groups)
   auto split_rows = [&]() -> int {
     int my = 0;
     for (int b = b0 + tid; b < b1; b += nthr) my += __ldg(a.counts + b);
@@ -627,189 +630,57 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const Sp
     for (int i = 0; i < nwarps; ++i) t += s_wsum[i];
     return t;
   };
-
-  const bool one_group = b1 - b0 <= nthr;
-  const int rows = one_group ? (b1 > b0 ? group_prefix(b0, b1 - b0) : 0) : split_rows();
-  const bool packed = __ldg(a.meta) != 0u && rows <= 65535;
-  uint32_t* __restrict__ part = a.part + (size_t)blockIdx.x * (size_t)a.tile_w;
-
-  // one group of compaction blocks: the warp's slices k = warp, warp + W, ..., flat rounds
-  auto run_group = [&](int g0, int total, auto pk, uint32_t lo) {
-    constexpr bool PACK = decltype(pk)::value;
-    const int nslices = (total + 31) >> 5;
-    if (nslices == 0) return;
-    const int gmax = max(total - 1, 0);
-    const int ng = min(nthr, b1 - g0);
-    auto block_of = [&](int g) -> int {
-      int l = 0, h = ng;
-      while (h - l > 1) {
-        const int mid = (l + h) >> 1;
-        if (s_boff[mid] <= g) l = mid;
-        else h = mid;
-      }
-      return l;
-    };
-    auto fetch_row = [&](int k, int& blk) -> int32_t {
-      const int g = (k << 5) + lane;
-      if (k >= nslices || g >= total) return -1;
-      while (s_boff[blk + 1] <= g) ++blk;
-      return __ldg(a.lists + (int64_t)(g0 + blk) * kCompactRows + (g - s_boff[blk]));
-    };
-    auto fetch_desc = [&](int32_t row, uint32_t& st, uint32_t& nch) {
-      st = 0;
-      nch = 0;
-      if (row >= 0) {
-        const uint32_t* so = a.seg_off + (int64_t)row * so_stride + tile;
-        st = __ldg(so);
-        nch = __ldg(so + 1) - st;
-      }
-    };
-    const uint32_t lane_le = lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u);
-    uint32_t s_d = 0, s_P = 0, s_C = 0, s_E = 0, s_n1 = 0, g_j = 0, g_base = 0;
-    auto prepare = [&](int kk, uint32_t st, uint32_t n) {
-      const bool valid = (kk << 5) + lane < total;
-      const uint32_t n1 = valid ? max(n, 1u) : 0u;
-      uint32_t incl = n1;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(FULL, incl, o);
-        if (lane >= o) incl += t;
-      }
-      s_C = __shfl_sync(FULL, incl, 31);
-      s_P = incl - n1;
-      s_d = st - s_P;
-      s_n1 = n1;
-      s_E = __ballot_sync(FULL, valid && n == 0u);
-      g_j = 0;
-      g_base = 0;
-    };
-    int k = warp;
-    int blk = block_of(min((k << 5) + lane, gmax));
-    uint32_t nst, nn;
-    {
-      uint32_t st0, n0;
-      fetch_desc(fetch_row(k, blk), st0, n0);            // slice k
-      fetch_desc(fetch_row(k + nwarps, blk), nst, nn);   // slice k + W
-      prepare(k, st0, n0);
+  // element j of the group's list of active rows (blocks g0 .. g0 + ng)
+  auto row_of = [&](int g0, int ng, int j) -> int32_t {
+    int l = 0, h = ng;
+    while (h - l > 1) {
+      const int mid = (l + h) >> 1;
+      if (s_boff[mid] <= j) l = mid;
+      else h = mid;
     }
-    int32_t row2 = fetch_row(k + 2 * nwarps, blk);     // slice k + 2W
-    bool live = k < nslices;
-    // the next round of the warp's stream (moving on to slice k + W when slice k is done): the
-    // chunk is loaded (or zero with lim = 0); false once every slice of the warp is distributed
-    auto load_rd = [&](uint4& v, uint32_t& lim) -> bool {
-      while (live && (g_j << 5) >= s_C) {
-        k += nwarps;
-        if (k >= nslices) {
-          live = false;
-          break;
-        }
-        prepare(k, nst, nn);
-        fetch_desc(row2, nst, nn);                      // slice k + W
-        row2 = fetch_row(k + 2 * nwarps, blk);          // slice k + 2W
-      }
-      v = make_uint4(0u, 0u, 0u, 0u);
-      lim = 0u;
-      if (!live) return false;
-      const uint32_t g = (g_j << 5) + lane;
-      const uint32_t contrib = ((s_P >> 5) == g_j && s_n1 > 0u) ? (1u << (s_P & 31u)) : 0u;
-      const uint32_t M = __reduce_or_sync(FULL, contrib);
-      const int o = ((int)(g_base + __popc(M & lane_le)) - 1) & 31;
-      g_base += __popc(M);
-      ++g_j;
-      const uint32_t dd = __shfl_sync(FULL, s_d, o);
-      if (g < s_C) {
-        lim = ((s_E >> o) & 1u) ? 0u : 1u;
-        v = ld_stream_u4(a.idx + 8ull * (g + dd));
-      }
-      return true;
-    };
-    auto add8 = [&](const uint4 v, uint32_t lim) {
-      const uint32_t x[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
-                             v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
-#pragma unroll
-      for (int e = 0; e < 8; ++e) {
-        if (PACK) {
-          // two columns a word: column x adds 1 to the low half (x even) or high half (x odd)
-          red_if(x[e], lim ? tile_w : 0u, acc_s + ((x[e] >> 1) << 2), (x[e] & 1u) ? 0x10000u : 1u);
-        } else {
-          const uint32_t y = x[e] - lo;  // columns [lo, lo + half_w) of this pass; the pad falls outside
-          red_if(y, lim ? (uint32_t)half_w : 0u, acc_s + (y << 2), 1u);
-        }
-      }
-    };
-    uint4 v[kSplitRounds + 1];
-    uint32_t lim[kSplitRounds + 1];
-    bool ok[kSplitRounds + 1];
-#pragma unroll
-    for (int i = 0; i < kSplitRounds; ++i) ok[i] = load_rd(v[i], lim[i]);
-    while (ok[0]) {
-      ok[kSplitRounds] = load_rd(v[kSplitRounds], lim[kSplitRounds]);
-      add8(v[0], lim[0]);
-#pragma unroll
-      for (int i = 0; i < kSplitRounds; ++i) {
-        v[i] = v[i + 1];
-        lim[i] = lim[i + 1];
-        ok[i] = ok[i + 1];
-      }
-    }
-  };
-  auto run_split = [&](auto pk, uint32_t lo) {
-    for (int g0 = b0; g0 < b1; g0 += nthr) {
-      const int total = one_group ? rows : group_prefix(g0, min(nthr, b1 - g0));
-      run_group(g0, total, pk, lo);
-    }
+    return __ldg(a.lists + (int64_t)(g0 + l) * kCompactRows + (j - s_boff[l]));
   };
 
-  // CTA-wide flat passes (16-bit counters, one group of blocks): up to kFlatRows rows and
-  // kFlatRounds * 32 chunks a pass.  Rounds go to warps round-robin, so the warps stay within
-  // a round of each other whatever the segment lengths.
-  auto run_flat = [&]() {
-    const int ng = b1 - b0;
+  // CTA-wide passes over the `total` active rows of one group: up to kFlatRows rows and
+  // kFlatRounds * 32 chunks a pass (a pass stops before a row that would overflow its rounds;
+  // a row longer than a whole pass goes through row_loop instead)
+  auto run_flat = [&](int g0, int ng, int total) {
     const uint32_t lane_le1 = (lane == 31 ? 0xFFFFFFFFu : ((2u << lane) - 1u)) & ~1u;
-    for (int i0 = 0; i0 < rows;) {
-      const int cnt = min(kFlatRows, rows - i0);
+    for (int i0 = 0; i0 < total;) {
+      const int cnt = min(kFlatRows, total - i0);
       __syncthreads();  // the previous pass's tables are no longer read
       for (int i = tid; i < kFlatRows / 32; i += nthr) t_emp[i] = 0u;
       if (tid == 0) s_cut = cnt;
       __syncthreads();
-      // segment bounds of rows i0 .. i0 + cnt (four rows a thread, loads issued together)
       {
-        uint32_t st[4], en[4];
+        uint32_t st[kFlatRows / kTiledThreads], en[kFlatRows / kTiledThreads];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < kFlatRows / kTiledThreads; ++k) {
           const int i = tid + k * nthr;
           st[k] = en[k] = 0u;
           if (i < cnt) {
-            const int j = i0 + i;
-            int l = 0, h = ng;
-            while (h - l > 1) {
-              const int mid = (l + h) >> 1;
-              if (s_boff[mid] <= j) l = mid;
-              else h = mid;
-            }
-            const int32_t row = __ldg(a.lists + (int64_t)(b0 + l) * kCompactRows + (j - s_boff[l]));
-            const uint32_t* so = a.seg_off + (int64_t)row * so_stride + tile;
+            const uint32_t* so = a.seg_off + (int64_t)row_of(g0, ng, i0 + i) * so_stride + tile;
             st[k] = __ldg(so);
             en[k] = __ldg(so + 1);
           }
         }
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < kFlatRows / kTiledThreads; ++k) {
           const int i = tid + k * nthr;
           if (i < cnt) {
             t_st[i] = st[k];
-            t_P[i] = max(en[k] - st[k], 1u);  // an empty segment takes one chunk, skipped
+            t_P[i] = max(en[k] - st[k], 1u);  // an empty segment takes one chunk of pads
             if (en[k] == st[k]) atomicOr(&t_emp[i >> 5], 1u << (i & 31));
           }
         }
       }
       __syncthreads();
-      // exclusive prefix of the chunk counts, four consecutive rows a thread
       {
-        uint32_t c[4], loc = 0;
+        constexpr int PER = kFlatRows / kTiledThreads;  // consecutive rows a thread
+        uint32_t c[PER], loc = 0;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const int i = 4 * tid + k;
+        for (int k = 0; k < PER; ++k) {
+          const int i = PER * tid + k;
           c[k] = i < cnt ? t_P[i] : 0u;
           loc += c[k];
         }
@@ -834,23 +705,28 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const Sp
         __syncthreads();
         uint32_t run = (uint32_t)s_wsum[warp] + incl - loc;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const int i = 4 * tid + k;
+        for (int k = 0; k < PER; ++k) {
+          const int i = PER * tid + k;
           if (i < cnt) {
             t_P[i] = run;
             run += c[k];
-            if (run > (uint32_t)(32 * kFlatRounds)) atomicMin(&s_cut, i);  // row i ends past the pass's rounds
+            if (run > (uint32_t)(32 * kFlatRounds)) atomicMin(&s_cut, i);  // row i ends past the pass
             if (i == cnt - 1) s_tot = run;
           }
         }
       }
       __syncthreads();
-      // a dup-free row fits a pass (its segment has at most tile_w / 8 + 1 chunks), so a pass
-      // takes at least one row
-      const int cut = max(s_cut, 1);
+      const int cut = s_cut;
+      if (cut == 0) {
+        // the pass's first row alone exceeds the tables (only a row holding columns many times
+        // can): its chunks go lane by lane, 8 lanes a chunk row
+        const uint32_t st = t_st[0], nch = (cut + 1 < cnt ? t_P[1] : s_tot);
+        if (!((t_emp[0] >> 0) & 1u))
+          for (uint32_t c = tid; c < nch; c += nthr) add8(ld_stream_u4(a.idx + 8ull * (st + c)));
+        i0 += 1;
+        continue;
+      }
       const uint32_t Ctot = cut < cnt ? t_P[cut] : s_tot;
-      // at most kFlatRounds: a pass ends before the row that would pass it, and a first row
-      // alone fits (see above); the clamp keeps the tables in bounds whatever the input
       const int nr = min((int)((Ctot + 31u) >> 5), kFlatRounds);
       for (int r = tid; r < nr; r += nthr) t_M[r] = 0u;
       __syncthreads();
@@ -860,63 +736,56 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const Sp
         for (uint32_t r = (p + 31u) >> 5; (r << 5) < e && r < (uint32_t)nr; ++r) t_first[r] = (uint32_t)i;
       }
       __syncthreads();
-      // rounds r = warp, warp + W, ...: lane l takes chunk 32 r + l; its owner is the segment of
-      // the round's first chunk plus the segment starts at positions 1 .. l of the round
-      auto round_load = [&](int r, uint4& v, uint32_t& lim) {
-        v = make_uint4(0u, 0u, 0u, 0u);
-        lim = 0u;
-        if (r >= nr) return;
+      // round r: lane l takes chunk 32 r + l, owned by the segment of the round's first chunk plus
+      // the segment starts at positions 1 .. l of the round
+      auto round_load = [&](int r) -> uint4 {
+        if (r >= nr) return pads;
         const uint32_t g = ((uint32_t)r << 5) + lane;
-        if (g < Ctot) {
-          const uint32_t o = min(t_first[r] + __popc(t_M[r] & lane_le1), (uint32_t)cut - 1u);
-          lim = ((t_emp[o >> 5] >> (o & 31u)) & 1u) ? 0u : tile_w;
-          v = ld_stream_u4(a.idx + 8ull * (t_st[o] + (g - t_P[o])));
-        }
+        if (g >= Ctot) return pads;
+        const uint32_t o = min(t_first[r] + __popc(t_M[r] & lane_le1), (uint32_t)cut - 1u);
+        if ((t_emp[o >> 5] >> (o & 31u)) & 1u) return pads;
+        return ld_stream_u4(a.idx + 8ull * (t_st[o] + (g - t_P[o])));
       };
-      uint4 v0, v1, v2;
-      uint32_t l0, l1, l2;
       int r = warp;
-      round_load(r, v0, l0);
-      round_load(r + nwarps, v1, l1);
+      uint4 v0 = round_load(r), v1 = round_load(r + nwarps);
       for (; r < nr; r += nwarps) {
-        round_load(r + 2 * nwarps, v2, l2);
-        const uint32_t x[8] = {v0.x & 0xFFFFu, v0.x >> 16, v0.y & 0xFFFFu, v0.y >> 16,
-                               v0.z & 0xFFFFu, v0.z >> 16, v0.w & 0xFFFFu, v0.w >> 16};
-#pragma unroll
-        for (int e = 0; e < 8; ++e)
-          red_if(x[e], l0, acc_s + ((x[e] >> 1) << 2), (x[e] & 1u) ? 0x10000u : 1u);
+        const uint4 v2 = round_load(r + 2 * nwarps);
+        add8(v0);
         v0 = v1;
-        l0 = l1;
         v1 = v2;
-        l1 = l2;
       }
       i0 += cut;
     }
   };
 
-  if (packed) {
-    if (one_group) run_flat();
-    else run_split(std::true_type{}, 0u);
-    __syncthreads();
-    const uint4* acc4 = reinterpret_cast<const uint4*>(acc);
-    uint4* p4 = reinterpret_cast<uint4*>(part);
-    for (int i = tid; i < (half_w >> 2); i += nthr) p4[i] = acc4[i];
+  const bool one_group = b1 - b0 <= nthr;
+  int rows;
+  if (one_group) {
+    rows = b1 > b0 ? group_prefix(b0, b1 - b0) : 0;
+    run_flat(b0, b1 - b0, rows);
   } else {
-    for (int pass = 0; pass < 2; ++pass) {
-      const uint32_t lo = (uint32_t)(pass * half_w);
-      run_split(std::false_type{}, lo);
-      __syncthreads();
-      const uint4* acc4 = reinterpret_cast<const uint4*>(acc);
-      uint4* p4 = reinterpret_cast<uint4*>(part + lo);
-      for (int i = tid; i < (half_w >> 2); i += nthr) p4[i] = acc4[i];
-      if (pass == 0) {
-        __syncthreads();
-        zero_acc();
-        __syncthreads();
-      }
+    rows = split_rows();
+    for (int g0 = b0; g0 < b1; g0 += nthr) {
+      const int ng = min(nthr, b1 - g0);
+      run_flat(g0, ng, group_prefix(g0, ng));
     }
   }
-  if (tid == 0) a.fmt[blockIdx.x] = packed ? 0u : 1u;
+  __syncthreads();
+  // the partial counts: 16-bit pairs when no column can have reached 65,536
+  const bool narrow = __ldg(a.meta) != 0u && rows <= 65535;
+  uint32_t* __restrict__ part = a.part + (size_t)blockIdx.x * (size_t)a.tile_w;
+  const uint4* acc4 = reinterpret_cast<const uint4*>(acc);
+  if (narrow) {
+    uint2* p2 = reinterpret_cast<uint2*>(part);
+    for (int i = tid; i < (a.tile_w >> 2); i += nthr) {
+      const uint4 c = acc4[i];
+      p2[i] = make_uint2(c.x | (c.y << 16), c.z | (c.w << 16));
+    }
+  } else {
+    uint4* p4 = reinterpret_cast<uint4*>(part);
+    for (int i = tid; i < (a.tile_w >> 2); i += nthr) p4[i] = acc4[i];
+  }
+  if (tid == 0) a.fmt[blockIdx.x] = narrow ? 0u : 1u;
 }
 
 // out[t * tile_w + c] = (float)(sum over the R splits of tile t of their count of column c) * w,
@@ -1254,12 +1123,8 @@ static bp_status tiled_args_from_plan(const bp_csr_plan* plan, int cluster, Tile
   return BP_OK;
 }
 
-// A plan whose tile of 32-bit counts does not fit one CTA's shared memory runs the split path
-// (16-bit counters, partial counts in the workspace); only homogeneous plans are built that way.
-static bool is_split_plan(const bp_csr_plan* plan) {
-  return plan->heter == 0 && plan->tile_w % 64 == 0 && plan->tile_w <= kSplitMaxTile &&
-         tiled_smem_bytes(acc_words_for(plan->tile_w, 1)) > (size_t)max_smem_optin() - kStaticSmemReserve;
-}
+// Counting plans (kind 1) run the split path: homogeneous weights, single event vectors.
+static bool is_split_plan(const bp_csr_plan* plan) { return plan->kind == 1; }
 
 // CTAs per tile of the split path: the tiles share the device's SMs, one CTA each
 static int split_count(const bp_csr_plan* plan) {
@@ -1352,6 +1217,7 @@ bp_status bp_csr_plan_build(const float* data, int64_t ndata, const void* indice
   p.tile_w = tile_w;
   p.n_tiles = (int32_t)nt;
   p.heter = heter ? 1 : 0;
+  p.kind = 0;
   p.entries = L.entries;
   p.mem = mem;
   p.bytes = bytes;
@@ -1444,6 +1310,10 @@ static bp_status planned_batch(const char* who, const bp_csr_plan* plan, const f
   const size_t need = bp_event_csrmv_planned_batch_workspace_size(plan, batch);
   BP_REQUIRE(workspace && workspace_bytes >= need, BP_ENOMEM, "%s: workspace %zu < %zu", who, workspace_bytes, need);
   if (is_split_plan(plan)) {
+    BP_REQUIRE(plan->heter == 0 && plan->tile_w % 32 == 0 &&
+                   split_smem_bytes(plan->tile_w) <= (size_t)max_smem_optin() - kStaticSmemReserve,
+               BP_EINVAL, "%s: a counting plan needs a homogeneous weight and a tile of at most %d columns "
+               "(bp_csr_plan_count_tile), got %d", who, bp_csr_plan_count_tile(plan->n > 0 ? plan->n : 1), plan->tile_w);
     BP_REQUIRE(!dense && batch == 1, BP_ENOTSUP,
                "%s: a plan of %d-column tiles (16-bit counters) serves one event vector a call; build a plan "
                "with a smaller tile (bp_csr_plan_default_tile) for dense vectors and batches", who, plan->tile_w);
@@ -1528,17 +1398,16 @@ static bp_status split_call(const bp_csr_plan* plan, const float* w_homo, const 
 extern "C" {
 
 int32_t bp_csr_plan_count_tile(int64_t n) {
-  // the split path pays off once a call reads few enough, large enough segments: at least
-  // 2^19 columns, tiles of at most kSplitMaxTile columns that still exceed one CTA's 32-bit
-  // accumulator
+  // worth it from 2^19 columns: tiles as wide as one CTA's shared memory holds 32-bit counts
+  // (beside the block offsets, the pass tables and the dummy words), in multiples of 64
   if (n < (1 << 19)) return 0;
-  const int64_t nt = (n + kSplitMaxTile - 1) / kSplitMaxTile;
+  const int64_t cap_bytes = (int64_t)max_smem_optin() - (int64_t)kStaticSmemReserve - 4 * (kBlockGroup + 1) -
+                            (int64_t)split_table_bytes() - 4 * kSplitDummy;
+  const int64_t cap = std::min<int64_t>(cap_bytes / 4 / 64 * 64, kPlanMaxTileW / 64 * 64);
+  const int64_t nt = (n + cap - 1) / cap;
   int64_t tw = (n + nt - 1) / nt;
   tw = (tw + 63) / 64 * 64;
-  if (tw > kSplitMaxTile) tw = kSplitMaxTile;
-  const int64_t cap = ((int64_t)max_smem_optin() - (int64_t)kStaticSmemReserve - 4 * (kBlockGroup + 1)) / 4;
-  if (tw <= cap) return 0;
-  return (int32_t)tw;
+  return (int32_t)std::min(tw, cap);
 }
 
 }  // extern "C"

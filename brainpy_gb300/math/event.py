@@ -59,6 +59,8 @@ class CSRPlan:
                              _lib.ptr(indptr), itype, indices.numel(), m, n, self.tile_w, _lib.ptr(self.mem),
                              nbytes, ctypes.byref(self.c), _lib.stream_handle(dev))
     _lib.check(st, "csr_plan_build")
+    if kind == "count":
+      self.c.kind = 1
     self.heter = bool(heter)
     self.device = dev
     # per-call state kept ready: the C plan struct, a unit weight, and one workspace per stream

@@ -200,21 +200,23 @@ typedef struct {
   uint64_t entries;   /* capacity of the padded index array */
   void* mem;          /* device memory holding the plan (caller-owned) */
   size_t bytes;       /* size of mem */
+  int32_t kind;       /* 0: general plan (cluster kernels; every product, batches, weights);
+                         1: counting plan (split kernels; homogeneous weight, one event vector a
+                         call; tile_w from bp_csr_plan_count_tile).  bp_csr_plan_build sets 0; the
+                         caller sets 1 on a homogeneous plan built with a counting tile. */
 } bp_csr_plan;
 
 /* tile width the tiled kernels run best with on the current device for n columns and
  * clusters of `cluster` CTAs (1, 2, 4 or 8); 0 on error. */
 int32_t bp_csr_plan_default_tile(int64_t n, int32_t cluster);
 /* tile width of a counting plan for n columns, 0 when n is too small for one (n < 2^19).
- * A counting plan has tiles of up to 65,472 columns, more than one CTA holds as 32-bit counts:
- * bp_event_csrmv_planned runs it with 16-bit counters, R CTAs per tile (R = SMs / n_tiles, at
- * most 16) and a second kernel that adds the R partial counts of every column (the workspace
- * holds them).  A call then reads half as many, twice as long segments as with the default
- * tile; DRAM serves random reads of up to ~128 bytes at a fixed rate, so the call is faster.
- * Counting plans serve homogeneous plans and single event vectors only (BP_ENOTSUP for dense
- * vectors and batches).  A CTA that could overflow a 16-bit count (a row holding a column
- * twice, or more than 65,535 active rows of its share) counts in 32 bits, two passes over its
- * rows. */
+ * A counting plan (bp_csr_plan.kind = 1) has tiles as wide as one CTA's shared memory holds
+ * 32-bit counts (about 50K columns).  bp_event_csrmv_planned runs it with R CTAs per tile
+ * (R = SMs / n_tiles, at most 16), each counting its share of the active rows, and a second
+ * kernel that adds the R partial counts of every column (the workspace holds them).  A call
+ * then reads fewer, longer segments than with the default tile: DRAM serves random reads of up
+ * to ~128 bytes at a fixed rate, so the call is faster.  Counting plans serve homogeneous
+ * weights and single event vectors (BP_ENOTSUP for dense vectors and batches). */
 int32_t bp_csr_plan_count_tile(int64_t n);
 size_t bp_csr_plan_bytes(int64_t m, int64_t n, int64_t nnz, int32_t heter, int32_t tile_w);
 /* The compiled tiled-kernel variants (bp_csr_plan.variant codes): writes up to `cap` codes into

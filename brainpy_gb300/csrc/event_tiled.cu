@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256) plan_build_kernel(const IdxT* __restrict_
       uint32_t h = hist[t], hp = (h + 7u) & ~7u;
       for (uint32_t p = h; p < hp; ++p) {
         uint64_t dst = rs + offs[t] + p;
-        idx[dst] = (uint16_t)tile_w;  // the pad index: one past the tile
+        idx[dst] = (uint16_t)(tile_w + (((dst >> 3) & 3u) << 3) + (dst & 7u));  // a pad index past the tile
         if (w) w[dst] = 0.0f;
       }
     }
@@ -219,7 +219,9 @@ __device__ __forceinline__ void accumulate8(uint32_t acc_s, uint4 v, float4 w0, 
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     const uint32_t ad = acc_s + 4u * x[q];
-    if (MODE == kCount) red_if(x[q], lim, ad, 1u);
+    // counts: every entry adds, pads to the dummy words past the tile (lanes without a chunk
+    // carry pads too), which saves the predicate (about half the add's instructions)
+    if (MODE == kCount) asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(ad));
     else if (MODE == kWeight) red_if(x[q], lim, ad, ww[q]);
     else if (MODE == kRowVal) red_if(x[q], lim, ad, xv);
     else red_if(x[q], lim, ad, __fmul_rn(ww[q], xv));
@@ -265,6 +267,8 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
   uint32_t* acc = reinterpret_cast<uint32_t*>(smem);
   const uint32_t acc_s = (uint32_t)__cvta_generic_to_shared(acc);
   const uint32_t tile_w = (uint32_t)a.tile_w;
+  const uint32_t lpad = (tile_w + (uint32_t)(threadIdx.x & 31)) * 0x10001u;  // this lane's dummy word, twice
+  const uint4 lane_pads = make_uint4(lpad, lpad, lpad, lpad);
   int* s_boff = reinterpret_cast<int*>(smem + sizeof(uint32_t) * (size_t)a.acc_words);  // kBlockGroup + 1
   __shared__ int s_wsum[32];
 
@@ -386,7 +390,8 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
           const bool in = c < U.ln[u];
           U.lim[u][r] = in ? tile_w : 0u;
           const uint64_t e = 8ull * (U.st[u] + (in ? c : 0u));
-          U.vv[u][r] = ld_stream_u4(a.idx + e);
+          if (MODE == kCount) U.vv[u][r] = in ? ld_stream_u4(a.idx + e) : lane_pads;
+          else U.vv[u][r] = ld_stream_u4(a.idx + e);
           if (HAS_W) {
             U.w0[u][r] = ld_stream_f4(a.w + e);
             U.w1[u][r] = ld_stream_f4(a.w + e + 4);
@@ -521,10 +526,10 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
 // counts the active rows of compaction blocks [q nb / R, (q + 1) nb / R) for its tile and
 // writes them to the workspace; split_reduce_kernel adds the R partial counts of a column and
 // writes (float)count * w.
-//   - Counting: one shared-memory add of 1 per entry, predicated on index < tile_w: the pad
-//     index tile_w, and every entry of an inactive lane or an empty segment (given a chunk of
-//     pads), add nothing.  (Sending them all to one dummy word instead made the lanes of an
-//     add instruction collide on that word: 30 % slower at 2 % events, 50 % at 10 %.)
+//   - Counting: one unpredicated shared-memory add of 1 per entry (half the instructions of a
+//     predicated add).  Pad entries land on the 32 dummy words past the tile (the plan spreads
+//     its pad values over them); an inactive lane or an empty segment gets a chunk of this
+//     lane's dummy word, so the lanes of one add instruction rarely meet on a word.
 //   - Work: the CTA tabulates its rows' segments in shared memory (start chunk, chunk prefix)
 //     and deals the flattened chunks out in rounds of 32, round r to warp r mod W, chunk
 //     32 r + l to lane l; the warps stay within a round of each other whatever the segment
@@ -534,7 +539,7 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
 constexpr int kFlatRows = 2048;    // rows a CTA-wide pass tabulates
 constexpr int kFlatRounds = 1024;  // rounds of 32 chunks a pass holds (32,768 chunks)
 constexpr int kSplitMaxSplits = 16;
-constexpr int kSplitDummy = 32;    // words past the tile (keeps the accumulator a multiple of 32 words)
+constexpr int kSplitDummy = kPlanPadSpan;  // dummy words past the tile, where pad entries add
 
 static size_t split_table_bytes() { return sizeof(uint32_t) * (size_t)(2 * kFlatRows + kFlatRows / 32 + 2 * kFlatRounds); }
 static size_t split_smem_bytes(int tile_w) {
@@ -552,12 +557,6 @@ struct SplitArgs {
   int64_t m, n;
   int32_t tile_w, n_tiles, nb, R;
 };
-
-// adds 1 to the word at shared address addr when x < lim (the pad index tile_w is skipped)
-__device__ __forceinline__ void red1_if(uint32_t x, uint32_t lim, uint32_t addr) {
-  asm volatile("{\n\t.reg .pred p;\n\tsetp.lt.u32 p, %0, %1;\n\t@p red.shared.add.u32 [%2], 1;\n\t}" ::"r"(x), "r"(lim),
-               "r"(addr));
-}
 
 __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const SplitArgs a) {
   constexpr unsigned FULL = 0xffffffffu;
@@ -580,8 +579,8 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const Sp
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarps = nthr >> 5;
   const uint32_t tile_w = (uint32_t)a.tile_w;
-  const uint32_t pad2 = tile_w | (tile_w << 16);
-  const uint4 pads = make_uint4(pad2, pad2, pad2, pad2);  // a chunk that adds only to the dummy word
+  const uint32_t pad2 = (tile_w + (uint32_t)lane) * 0x10001u;
+  const uint4 pads = make_uint4(pad2, pad2, pad2, pad2);  // a chunk that adds only to this lane's dummy word
   const int64_t so_stride = a.n_tiles + 1;
   {
     uint4* acc4 = reinterpret_cast<uint4*>(acc);
@@ -596,7 +595,7 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const Sp
     const uint32_t x[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
                            v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
 #pragma unroll
-    for (int e = 0; e < 8; ++e) red1_if(x[e], tile_w, acc_s + (x[e] << 2));
+    for (int e = 0; e < 8; ++e) asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(acc_s + (x[e] << 2)));
   };
   // exclusive prefix of the active-row counts of blocks [g0, g0 + ng) into s_boff; returns the total
   auto group_prefix = [&](int g0, int ng) -> int {
@@ -884,9 +883,11 @@ static size_t tiled_smem_bytes(int acc_words) {
   return sizeof(uint32_t) * (size_t)acc_words + sizeof(int) * (kBlockGroup + 1);
 }
 
+// the tile's counters plus kPlanPadSpan dummy words (where unpredicated adds of pad entries
+// land), rounded up to a multiple of 4 words per rank
 static int acc_words_for(int tile_w, int R) {
   int q = 4 * R;
-  return (tile_w + q - 1) / q * q;
+  return (tile_w + kPlanPadSpan + q - 1) / q * q;
 }
 
 // Raises a kernel's dynamic shared-memory limit to the largest size any launch uses (once per
@@ -1016,12 +1017,12 @@ __global__ void __launch_bounds__(1024) csrmv_n_planned_kernel(const uint32_t* _
                                                                const float* __restrict__ w, const float* __restrict__ x,
                                                                int64_t m, int64_t n, int32_t tile_w, int32_t n_tiles,
                                                                int32_t splits, float* __restrict__ part) {
-  extern __shared__ float xs[];  // tile_w + 1: xs[tile_w] = 0 is what the pad index reads
+  extern __shared__ float xs[];  // tile_w + kPlanPadSpan: the pad indices read zeros
   const int t = blockIdx.x % n_tiles;
   const int sp = blockIdx.x / n_tiles;
   const int64_t col0 = (int64_t)t * tile_w;
   for (int k = threadIdx.x; k < tile_w; k += blockDim.x) xs[k] = col0 + k < n ? __ldg(x + col0 + k) : 0.0f;
-  if (threadIdx.x == 0) xs[tile_w] = 0.0f;
+  if (threadIdx.x < kPlanPadSpan) xs[tile_w + threadIdx.x] = 0.0f;
   __syncthreads();
   const int64_t r0 = (int64_t)sp * m / splits, r1 = (int64_t)(sp + 1) * m / splits;
   const int64_t so_stride = (int64_t)n_tiles + 1;
@@ -1052,7 +1053,7 @@ __global__ void __launch_bounds__(1024) csrmv_n_planned_kernel(const uint32_t* _
         const float4 w0 = __ldg(reinterpret_cast<const float4*>(w + 8ull * c));
         const float4 w1 = __ldg(reinterpret_cast<const float4*>(w + 8ull * c + 4));
         const float ww[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
-        // pad entries read xs[tile_w] = 0 with a zero weight: they add +0 (acc starts at +0
+        // pad entries read a zero past the tile with a zero weight: they add +0 (acc starts at +0
         // and a sum of floats is never -0 unless every term is), no test needed
 #pragma unroll
         for (int k = 0; k < 8; ++k) acc = fmaf(ww[k], xs[q[k]], acc);
@@ -1176,7 +1177,7 @@ int32_t bp_csr_plan_default_tile(int64_t n, int32_t cluster) {
   if (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8) cluster = 4;
   const int64_t cap_words =
       ((int64_t)max_smem_optin() - (int64_t)kStaticSmemReserve - 4 * (kBlockGroup + 1)) / 4;
-  const int64_t cap_tw = std::min<int64_t>(cap_words / 64 * 64, kPlanMaxTileW / 64 * 64);
+  const int64_t cap_tw = std::min<int64_t>((cap_words - kPlanPadSpan - 32) / 64 * 64, kPlanMaxTileW / 64 * 64);
   // how many clusters of `cluster` CTAs (one CTA per SM) can be resident at once
   int clusters = max_active_clusters(cluster, tiled_smem_bytes(acc_words_for((int)cap_tw, cluster)));
   if (clusters < 1) clusters = std::max(1, device_sm_count() / cluster);
@@ -1469,7 +1470,7 @@ bp_status bp_csrmv_planned_n(const bp_csr_plan* plan, const float* w_homo, const
   const size_t need = bp_csrmv_planned_n_workspace_size(plan);
   BP_REQUIRE(workspace && workspace_bytes >= need, BP_ENOMEM, "csrmv_planned_n: workspace %zu < %zu", workspace_bytes,
              need);
-  const size_t smem = sizeof(float) * ((size_t)plan->tile_w + 1);
+  const size_t smem = sizeof(float) * ((size_t)plan->tile_w + kPlanPadSpan);
   BP_REQUIRE(smem <= (size_t)max_smem_optin() - kStaticSmemReserve, BP_ENOTSUP,
              "csrmv_planned_n: tile of %d columns does not fit shared memory", plan->tile_w);
   PlanView v = plan_view(plan);

@@ -3,9 +3,11 @@
 // For a CSR matrix of shape m x n the output columns are cut into n_tiles tiles of
 // tile_w columns.  Every row's column indices are regrouped by tile; the group of
 // row r for tile t (a "segment") holds tile-local uint16 indices (col - t*tile_w) and
-// is padded with the index tile_w (one past the tile: every kernel's `< tile_w` test skips
-// it, and a gather from a shared-memory tile with a zero at tile_w adds nothing) to a
-// multiple of 8 entries, so that every segment is a whole
+// is padded to a multiple of 8 entries with pad indices in [tile_w, tile_w + 32): entry slot
+// e of chunk c holds tile_w + 8 * (c & 3) + e.  Every kernel's `< tile_w` test skips them, a
+// gather from a shared-memory tile with 32 zeros past it adds nothing, and unpredicated
+// shared-memory adds land on 32 dummy words past the tile, spread over 32 banks so that the
+// lanes of one add instruction rarely meet on one word.  So every segment is a whole
 // number of 16-byte chunks starting on a 16-byte boundary (a valid bulk-copy source).
 // Heterogeneous weights are permuted along (float32, zero padding, same positions:
 // chunk c holds weights [8c, 8c + 8), 32 bytes).
@@ -28,7 +30,8 @@
 namespace bp {
 
 constexpr int kPlanMaxTiles = 4000;  // plan build keeps 3 x n_tiles words in 48 KB of shared memory
-constexpr int kPlanMaxTileW = 65535;  // local indices and the pad value tile_w are uint16
+constexpr int kPlanMaxTileW = 65472;  // local indices and the pad values (below tile_w + 32) are uint16
+constexpr int kPlanPadSpan = 32;       // pad values tile_w + 8 * (chunk & 3) + slot: 32 distinct
 constexpr int kChunkEntries = 8;      // entries per 16-byte chunk
 constexpr int kPlanDupCheckMax = 4096;  // rows up to this length are checked for repeated columns
 

@@ -244,9 +244,10 @@ _ROUTES = {}  # matrix key -> (weak refs, versions, route)
 _PLAN_MIN_N = int(os.environ.get("BPGPU_PLAN_MIN_N", 1 << 15))
 _PLAN_MIN_NNZ = int(os.environ.get("BPGPU_PLAN_MIN_NNZ", 1 << 20))
 _PLAN_DISABLE = os.environ.get("BPGPU_DISABLE_PLAN", "0") == "1"
-# homogeneous event products on at least this many columns take the split plan (tiles of up
-# to 65,472 columns, 16-bit counters): half the segment reads of the general plan
-_SPLIT_MIN_N = int(os.environ.get("BPGPU_SPLIT_MIN_N", 1 << 19))
+# homogeneous event products on at least this many columns take the counting plan by default
+# (BPGPU_SPLIT_MIN_N; off unless set: the autotuner times it against the general plan and
+# routes a matrix to it when it wins)
+_SPLIT_MIN_N = int(os.environ.get("BPGPU_SPLIT_MIN_N", 1 << 62))
 
 
 def _ident(t):

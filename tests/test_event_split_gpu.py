@@ -61,8 +61,11 @@ def test_count_plan_matches_oracle(ev, orc, rate, kind):
   for fn, rule in ((ev.csrmv, orc.EV_F32_POS), (ev.csrmv_taichi, orc.EV_F32_NZ)):
     y = fn(0.75, ind, ptr, e, shape=(m, n), transpose=True).cpu().numpy()
     np.testing.assert_array_equal(y, _want(orc, 0.75, ind, ptr, events, (m, n), rule))
-  key = (ev._matrix_key(torch.tensor([0.75]), ind, ptr, m, n), "count")
-  assert key in ev._PLANS and ev._PLANS[key][2].kind == "count"
+  plan = ev.CSRPlan(ind, ptr, (m, n), kind="count")
+  e32 = torch.tensor([0.75], device="cuda")
+  np.testing.assert_array_equal(plan.csrmv(e, e32).cpu().numpy(), _want(orc, 0.75, ind, ptr, events, (m, n), orc.EV_F32_POS))
+  np.testing.assert_array_equal(plan.csrmv(e, e32, float_rule=2).cpu().numpy(),
+                                _want(orc, 0.75, ind, ptr, events, (m, n), orc.EV_F32_NZ))
 
 
 def test_count_plan_unaligned_output_and_int64(ev, orc):

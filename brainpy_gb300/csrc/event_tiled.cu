@@ -520,30 +520,35 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
 // split accumulation: counting plans (homogeneous weight, events)
 // ---------------------------------------------------------------------------
 // DRAM serves random reads of up to ~128 bytes at a fixed rate of row activations, so the
-// number of segment reads sets a call's floor.  A counting plan's tiles are as wide as a
-// CTA's shared memory holds 32-bit counts (~50K columns, 20 tiles at N = 1e6, against the
-// cluster path's ~28K columns), so a call reads fewer, longer segments.  CTA (tile t, split q)
+// number of segment reads sets a call's floor.  A counting plan's tiles are up to 65,472
+// columns wide (16 tiles at N = 1e6, against the cluster path's ~28K columns), so a call reads
+// fewer, longer segments.  CTA (tile t, split q)
 // counts the active rows of compaction blocks [q nb / R, (q + 1) nb / R) for its tile and
 // writes them to the workspace; split_reduce_kernel adds the R partial counts of a column and
 // writes (float)count * w.
-//   - Counting: one unpredicated shared-memory add of 1 per entry (half the instructions of a
-//     predicated add).  Pad entries land on the 32 dummy words past the tile (the plan spreads
-//     its pad values over them); an inactive lane or an empty segment gets a chunk of this
-//     lane's dummy word, so the lanes of one add instruction rarely meet on a word.
+//   - Counting: 16-bit counters, two columns a word, one unpredicated shared-memory add per
+//     entry (a predicated add costs twice the instructions).  Pad entries land on the 32 pad
+//     columns past the tile (the plan spreads its pad values over them); an inactive lane or an
+//     empty segment gets a chunk of this lane's pad column, so the lanes of one add
+//     instruction rarely meet on a word.  A CTA that could overflow a 16-bit count (a row
+//     holding a column twice, or more than 65,535 active rows in its share) counts in 32 bits
+//     instead, two passes over its rows, one for each half of the tile.
 //   - Work: the CTA tabulates its rows' segments in shared memory (start chunk, chunk prefix)
 //     and deals the flattened chunks out in rounds of 32, round r to warp r mod W, chunk
 //     32 r + l to lane l; the warps stay within a round of each other whatever the segment
 //     lengths, and the loads of the next rounds are in flight while a round's adds issue.
-//   - Partial counts are written as 16-bit pairs when no column can reach 65,536 in one CTA
-//     (no repeated column in any row, at most 65,535 active rows), as 32-bit counts otherwise.
-constexpr int kFlatRows = 2048;    // rows a CTA-wide pass tabulates
+//   - Partial counts are written as the 16-bit pairs, or as 32-bit counts in the 32-bit mode.
+constexpr int kFlatRows = 4096;    // rows a CTA-wide pass tabulates
 constexpr int kFlatRounds = 1024;  // rounds of 32 chunks a pass holds (32,768 chunks)
 constexpr int kSplitMaxSplits = 16;
-constexpr int kSplitDummy = kPlanPadSpan;  // dummy words past the tile, where pad entries add
+constexpr int kSplitMaxTile = 65472;  // a multiple of 64; pads reach tile_w + 31 < 65536
 
+// accumulator words: the tile and its 32 pad columns as 16-bit pairs (or, in the 32-bit mode,
+// one half of the tile's columns), a multiple of 4
+__host__ __device__ inline int split_acc_words(int tile_w) { return ((tile_w + kPlanPadSpan) / 2 + 3) / 4 * 4; }
 static size_t split_table_bytes() { return sizeof(uint32_t) * (size_t)(2 * kFlatRows + kFlatRows / 32 + 2 * kFlatRounds); }
 static size_t split_smem_bytes(int tile_w) {
-  return sizeof(uint32_t) * (size_t)(tile_w + kSplitDummy) + sizeof(int) * (kBlockGroup + 1) + split_table_bytes();
+  return sizeof(uint32_t) * (size_t)split_acc_words(tile_w) + sizeof(int) * (kBlockGroup + 1) + split_table_bytes();
 }
 
 struct SplitArgs {
@@ -561,7 +566,8 @@ struct SplitArgs {
 __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const SplitArgs a) {
   constexpr unsigned FULL = 0xffffffffu;
   extern __shared__ __align__(16) unsigned char smem[];
-  const int acc_words = a.tile_w + kSplitDummy;  // a multiple of 32
+  const int acc_words = split_acc_words(a.tile_w);
+  const int half_w = a.tile_w >> 1;  // columns of one half of the tile (the 32-bit mode's passes)
   uint32_t* acc = reinterpret_cast<uint32_t*>(smem);
   const uint32_t acc_s = (uint32_t)__cvta_generic_to_shared(acc);
   int* s_boff = reinterpret_cast<int*>(acc + acc_words);  // kBlockGroup + 1
@@ -591,11 +597,25 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const Sp
   // the compaction kernel of this call may still be running (programmatic dependent launch)
   cudaGridDependencySynchronize();
 
+  // 16-bit pairs: column x adds 1 to the low (x even) or high (x odd) half of word x / 2; pads
+  // land on the pairs past the tile.  32-bit mode: columns [lo, lo + half_w) only.
+  uint32_t lo = 0;
+  bool wide = false;
   auto add8 = [&](const uint4 v) {
     const uint32_t x[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
                            v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
+    if (!wide) {
 #pragma unroll
-    for (int e = 0; e < 8; ++e) asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(acc_s + (x[e] << 2)));
+      for (int e = 0; e < 8; ++e)
+        asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(acc_s + ((x[e] >> 1) << 2)), "r"(1u << ((x[e] & 1u) << 4)));
+    } else {
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const uint32_t y = x[e] - lo;
+        asm volatile("{\n\t.reg .pred p;\n\tsetp.lt.u32 p, %0, %1;\n\t@p red.shared.add.u32 [%2], 1;\n\t}" ::"r"(y),
+                     "r"((uint32_t)half_w), "r"(acc_s + (y << 2)));
+      }
+    }
   };
   // exclusive prefix of the active-row counts of blocks [g0, g0 + ng) into s_boff; returns the total
   auto group_prefix = [&](int g0, int ng) -> int {
@@ -764,33 +784,42 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const Sp
   };
 
   const bool one_group = b1 - b0 <= nthr;
-  int rows;
-  if (one_group) {
-    rows = b1 > b0 ? group_prefix(b0, b1 - b0) : 0;
-    run_flat(b0, b1 - b0, rows);
-  } else {
-    rows = split_rows();
-    for (int g0 = b0; g0 < b1; g0 += nthr) {
-      const int ng = min(nthr, b1 - g0);
-      run_flat(g0, ng, group_prefix(g0, ng));
-    }
-  }
-  __syncthreads();
-  // the partial counts: 16-bit pairs when no column can have reached 65,536
-  const bool narrow = __ldg(a.meta) != 0u && rows <= 65535;
+  const int rows = one_group ? (b1 > b0 ? group_prefix(b0, b1 - b0) : 0) : split_rows();
+  // 16-bit pairs are exact while no column gets 65,536 adds: no row holds a column twice and
+  // the CTA sees at most 65,535 active rows.  Otherwise two passes of 32-bit counts, one for
+  // each half of the tile.
+  wide = !(__ldg(a.meta) != 0u && rows <= 65535);
   uint32_t* __restrict__ part = a.part + (size_t)blockIdx.x * (size_t)a.tile_w;
-  const uint4* acc4 = reinterpret_cast<const uint4*>(acc);
-  if (narrow) {
-    uint2* p2 = reinterpret_cast<uint2*>(part);
-    for (int i = tid; i < (a.tile_w >> 2); i += nthr) {
-      const uint4 c = acc4[i];
-      p2[i] = make_uint2(c.x | (c.y << 16), c.z | (c.w << 16));
+  auto run_all = [&]() {
+    if (one_group) {
+      run_flat(b0, b1 - b0, rows);
+    } else {
+      for (int g0 = b0; g0 < b1; g0 += nthr) {
+        const int ng = min(nthr, b1 - g0);
+        run_flat(g0, ng, group_prefix(g0, ng));
+      }
     }
-  } else {
+    __syncthreads();
+  };
+  const uint4* acc4 = reinterpret_cast<const uint4*>(acc);
+  if (!wide) {
+    run_all();
     uint4* p4 = reinterpret_cast<uint4*>(part);
-    for (int i = tid; i < (a.tile_w >> 2); i += nthr) p4[i] = acc4[i];
+    for (int i = tid; i < (a.tile_w >> 3); i += nthr) p4[i] = acc4[i];  // tile_w / 2 words of pairs
+  } else {
+    for (int pass = 0; pass < 2; ++pass) {
+      lo = (uint32_t)(pass * half_w);
+      run_all();
+      uint4* p4 = reinterpret_cast<uint4*>(part + lo);
+      for (int i = tid; i < (half_w >> 2); i += nthr) p4[i] = acc4[i];
+      if (pass == 0) {
+        __syncthreads();
+        uint4* z4 = reinterpret_cast<uint4*>(acc);
+        for (int i = tid; i < (acc_words >> 2); i += nthr) z4[i] = make_uint4(0u, 0u, 0u, 0u);
+      }
+    }
   }
-  if (tid == 0) a.fmt[blockIdx.x] = narrow ? 0u : 1u;
+  if (tid == 0) a.fmt[blockIdx.x] = wide ? 1u : 0u;
 }
 
 // out[t * tile_w + c] = (float)(sum over the R splits of tile t of their count of column c) * w,
@@ -1317,7 +1346,7 @@ static bp_status planned_batch(const char* who, const bp_csr_plan* plan, const f
   const size_t need = bp_event_csrmv_planned_batch_workspace_size(plan, batch);
   BP_REQUIRE(workspace && workspace_bytes >= need, BP_ENOMEM, "%s: workspace %zu < %zu", who, workspace_bytes, need);
   if (is_split_plan(plan)) {
-    BP_REQUIRE(plan->heter == 0 && plan->tile_w % 32 == 0 &&
+    BP_REQUIRE(plan->heter == 0 && plan->tile_w % 64 == 0 && plan->tile_w <= kSplitMaxTile &&
                    split_smem_bytes(plan->tile_w) <= (size_t)max_smem_optin() - kStaticSmemReserve,
                BP_EINVAL, "%s: a counting plan needs a homogeneous weight and a tile of at most %d columns "
                "(bp_csr_plan_count_tile), got %d", who, bp_csr_plan_count_tile(plan->n > 0 ? plan->n : 1), plan->tile_w);
@@ -1405,16 +1434,15 @@ static bp_status split_call(const bp_csr_plan* plan, const float* w_homo, const 
 extern "C" {
 
 int32_t bp_csr_plan_count_tile(int64_t n) {
-  // worth it from 2^19 columns: tiles as wide as one CTA's shared memory holds 32-bit counts
-  // (beside the block offsets, the pass tables and the dummy words), in multiples of 64
+  // worth it from 2^19 columns: the fewest tiles of at most kSplitMaxTile columns, in multiples
+  // of 64, whose 16-bit accumulator and pass tables fit one CTA
   if (n < (1 << 19)) return 0;
-  const int64_t cap_bytes = (int64_t)max_smem_optin() - (int64_t)kStaticSmemReserve - 4 * (kBlockGroup + 1) -
-                            (int64_t)split_table_bytes() - 4 * kSplitDummy;
-  const int64_t cap = std::min<int64_t>(cap_bytes / 4 / 64 * 64, kPlanMaxTileW / 64 * 64);
-  const int64_t nt = (n + cap - 1) / cap;
+  const int64_t nt = (n + kSplitMaxTile - 1) / kSplitMaxTile;
   int64_t tw = (n + nt - 1) / nt;
   tw = (tw + 63) / 64 * 64;
-  return (int32_t)std::min(tw, cap);
+  if (tw > kSplitMaxTile) tw = kSplitMaxTile;
+  if (split_smem_bytes((int)tw) > (size_t)max_smem_optin() - kStaticSmemReserve) return 0;
+  return (int32_t)tw;
 }
 
 }  // extern "C"

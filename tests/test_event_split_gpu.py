@@ -1,10 +1,10 @@
 """event.csrmv (transpose) on counting plans against the oracle.
 
-A counting plan cuts the columns into tiles as wide as a CTA's shared memory holds 32-bit
-counts (20 tiles at N = 1e6), R CTAs per tile each count a share of the active rows, and a
-second kernel adds the R partial counts of every column.  Homogeneous weights: bit-exact
-against the oracle's count form ((float)count * w), including partial counts written in 32
-bits (a row holding a column twice, or more than 65,535 active rows in one CTA's share)."""
+A counting plan cuts the columns into tiles of up to 65,472 (16 at N = 1e6), R CTAs per tile
+each count a share of the active rows with 16-bit counters, and a second kernel adds the R
+partial counts of every column.  Homogeneous weights: bit-exact against the oracle's count form
+((float)count * w), including the 32-bit mode a CTA takes when a row holds a column twice or
+when its share of active rows exceeds 65,535."""
 import numpy as np
 import pytest
 import torch
@@ -39,9 +39,9 @@ def test_count_plan_layout(ev):
   L = _lib.lib()
   assert L.bp_csr_plan_count_tile(1 << 18) == 0
   tw = L.bp_csr_plan_count_tile(10 ** 6)
-  # as wide as a CTA's shared memory holds 32-bit counts: about twice the general plan's tile
-  assert tw % 64 == 0 and 40_000 < tw and 4 * tw < 227 * 1024
-  assert tw > 1.5 * L.bp_csr_plan_default_tile(10 ** 6, 4)
+  # up to 65,472 columns (16 tiles at N = 1e6): more than twice the general plan's tile
+  assert tw % 64 == 0 and tw <= 65_472 and -(-10 ** 6 // tw) == 16
+  assert tw > 2 * L.bp_csr_plan_default_tile(10 ** 6, 4)
   ind, ptr = fixed_prob_csr(2000, 600_000, 50, seed=1)
   plan = ev.CSRPlan(ind, ptr, (2000, 600_000), kind="count")
   assert plan.kind == "count" and plan.tile_w == L.bp_csr_plan_count_tile(600_000)
@@ -81,8 +81,8 @@ def test_count_plan_unaligned_output_and_int64(ev, orc):
 
 
 def test_count_plan_repeated_columns(ev, orc):
-  """Rows that hold a column more than once: the plan records it and every CTA writes its
-  partial counts in 32 bits."""
+  """Rows that hold a column more than once: the plan records it and every CTA counts in 32
+  bits, two passes over its rows (one for each half of the tile)."""
   m, n, k = 3000, 600_000, 300
   g = torch.Generator(device="cpu").manual_seed(7)
   ind = torch.randint(0, n, (m * k,), generator=g, dtype=torch.int32)
@@ -99,7 +99,7 @@ def test_count_plan_repeated_columns(ev, orc):
 
 
 def test_count_plan_many_active_rows(ev, orc):
-  """More than 65,535 active rows for one CTA: 32-bit partial counts, exact."""
+  """More than 65,535 active rows for one CTA: 32-bit counting, exact."""
   from brainpy_gb300.connect import fixed_prob_csr
   m, n, k = 2_000_000, 600_000, 2
   ind, ptr = fixed_prob_csr(m, n, k, seed=9)

@@ -248,7 +248,6 @@ struct TiledArgs {
   int32_t batch;    // vectors per launch: gridDim.y
   int32_t variant;  // the plan's chosen kernel variant (0: from the segment length)
   int32_t vec_out;  // every vector's out row is 16-byte aligned (tile_w is a multiple of 4)
-  const uint32_t* meta;  // plan meta: meta[0] != 0 when no row holds a column twice
 };
 
 // Warp-independent processing: after one CTA-wide prefix over this rank's compaction blocks,
@@ -296,7 +295,6 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
   // the compaction kernel of this call may still be running (programmatic dependent launch)
   cudaGridDependencySynchronize();
 
-  int rows_seen = 0;  // active rows this CTA counted
   // groups of at most one compaction block per thread (nthr <= kBlockGroup)
   for (int g0 = b0; g0 < b1; g0 += nthr) {
     const int ng = min(nthr, b1 - g0);
@@ -325,7 +323,6 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
     __syncthreads();
     const int total = s_boff[ng];
     const int nslices = (total + 31) >> 5;
-    rows_seen += total;
 
     auto block_of = [&](int g) -> int {
       int lo = 0, hi = ng;
@@ -459,35 +456,6 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
   }
 
   // ---- reduce the cluster's accumulators and write the tile
-  // Counts travel through distributed shared memory as 16-bit pairs when no column can have
-  // reached 65,536 in this CTA (no row holds a column twice, at most 65,535 rows counted):
-  // half the bytes of the exchange, which its bandwidth bounds.  Packed in place: every thread
-  // holds its words in registers across a barrier, then writes the pairs to the front.
-  __shared__ int s_narrow;
-  if (MODE == kCount) {
-    constexpr int KMAX = 8;  // uint4 a thread held across the barrier
-    const bool narrow = a.meta != nullptr && __ldg(a.meta) != 0u && rows_seen <= 65535 &&
-                        (a.acc_words >> 2) <= KMAX * nthr;
-    if (tid == 0) s_narrow = narrow ? 1 : 0;
-    if (narrow) {
-      uint4* acc4 = reinterpret_cast<uint4*>(acc);
-      const int n4 = a.acc_words >> 2;
-      uint4 hold[KMAX];
-      __syncthreads();  // every warp's adds are done
-#pragma unroll
-      for (int k = 0; k < KMAX; ++k) {
-        const int i = tid + k * nthr;
-        hold[k] = i < n4 ? acc4[i] : make_uint4(0u, 0u, 0u, 0u);
-      }
-      __syncthreads();
-      uint2* acc2 = reinterpret_cast<uint2*>(acc);
-#pragma unroll
-      for (int k = 0; k < KMAX; ++k) {
-        const int i = tid + k * nthr;
-        if (i < n4) acc2[i] = make_uint2(hold[k].x | (hold[k].y << 16), hold[k].z | (hold[k].w << 16));
-      }
-    }
-  }
   cluster.sync();
   const int slice = a.acc_words / R;  // multiple of 4
   const int c0 = rank * slice;
@@ -497,16 +465,8 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
   for (int c = c0 + 4 * tid; c < c0 + slice; c += 4 * nthr) {
     uint4 x[8];
 #pragma unroll
-    for (int r = 0; r < 8; ++r) {
-      if (r < R) {
-        if (MODE == kCount && *cluster.map_shared_rank(&s_narrow, r)) {
-          const uint2 p2 = *reinterpret_cast<const uint2*>(cluster.map_shared_rank(acc, r) + (c >> 1));
-          x[r] = make_uint4(p2.x & 0xFFFFu, p2.x >> 16, p2.y & 0xFFFFu, p2.y >> 16);
-        } else {
-          x[r] = *reinterpret_cast<const uint4*>(cluster.map_shared_rank(acc, r) + c);
-        }
-      }
-    }
+    for (int r = 0; r < 8; ++r)
+      if (r < R) x[r] = *reinterpret_cast<const uint4*>(cluster.map_shared_rank(acc, r) + c);
     float o[4];
     if (MODE == kCount) {
       uint4 s = make_uint4(0, 0, 0, 0);
@@ -1186,7 +1146,6 @@ static bp_status tiled_args_from_plan(const bp_csr_plan* plan, int cluster, Tile
   a.seg_off = v.seg_off;
   a.idx = v.idx;
   a.w = v.w;
-  a.meta = v.meta;
   a.batch = 1;
   a.variant = plan->variant;
   a.m = plan->m;

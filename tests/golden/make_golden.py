@@ -21,6 +21,7 @@ writes tests/golden/*.npz.  The fixtures are committed; tests never need the
 reference tree.
 """
 import ast
+import inspect
 import math
 import os
 import sys
@@ -431,6 +432,313 @@ def gen_plasticity():
   return out
 
 
+# --------------------------------------------------------------------------
+# consumer: LifRefLTC / LifRef, Expon, COBA, exponential Euler, VarDelay
+# --------------------------------------------------------------------------
+DYN = os.path.join(REF, "brainpy", "_src")
+
+
+def load_class(path, cls, names, bases, ns):
+  """Defines class `cls` in `ns` from the reference's own methods `names` of that class in
+  `path`, on the stand-in `bases` (names looked up in ns)."""
+  tree = ast.parse(open(path).read())
+  node = next((n for n in tree.body if isinstance(n, ast.ClassDef) and n.name == cls), None)
+  if node is None:
+    raise RuntimeError(f"{path}: no class {cls}")
+  body = [n for n in node.body if isinstance(n, ast.FunctionDef) and n.name in names]
+  if {n.name for n in body} != set(names):
+    raise RuntimeError(f"{path}: {cls} lacks some of {names}")
+  for n in body:
+    strip_annotations(n)
+  cdef = ast.ClassDef(name=cls, bases=[ast.Name(id=b, ctx=ast.Load()) for b in bases], keywords=[], body=body,
+                      decorator_list=[], type_params=[])
+  mod = ast.fix_missing_locations(ast.Module(body=[cdef], type_ignores=[]))
+  exec(compile(mod, path, "exec"), ns)
+  return ns[cls]
+
+
+def load_method(path, cls, name):
+  """The reference's method `name` of class `cls` as a module-level function definition."""
+  tree = ast.parse(open(path).read())
+  node = next(n for n in tree.body if isinstance(n, ast.ClassDef) and n.name == cls)
+  fn = next(n for n in node.body if isinstance(n, ast.FunctionDef) and n.name == name)
+  return strip_annotations(fn)
+
+
+def strip_annotations(fn):
+  """Drops decorators and type annotations (their names live in modules not loaded here)."""
+  fn.decorator_list = []
+  fn.returns = None
+  a = fn.args
+  for arg in a.posonlyargs + a.args + a.kwonlyargs + ([a.vararg] if a.vararg else []) + ([a.kwarg] if a.kwarg else []):
+    arg.annotation = None
+  return fn
+
+
+class Dual:
+  """Forward-mode dual number over float32 arrays: the stand-in for JAX's JVP inside
+  bm.vector_grad (the expressions it differentiates use -, +, *, / only)."""
+  __array_ufunc__ = None  # numpy operands defer to the reflected operators below
+
+  def __init__(self, v, d):
+    self.v = np.asarray(v, np.float32)
+    self.d = np.asarray(d, np.float32)
+
+  @staticmethod
+  def _vd(o):
+    return (o.v, o.d) if isinstance(o, Dual) else (o, None)
+
+  def __neg__(self):
+    return Dual(-self.v, -self.d)
+
+  def __add__(self, o):
+    ov, od = self._vd(o)
+    return Dual(self.v + ov, self.d if od is None else self.d + od)
+
+  __radd__ = __add__
+
+  def __sub__(self, o):
+    ov, od = self._vd(o)
+    return Dual(self.v - ov, self.d if od is None else self.d - od)
+
+  def __rsub__(self, o):
+    return Dual(o - self.v, -self.d)
+
+  def __mul__(self, o):
+    ov, od = self._vd(o)
+    return Dual(self.v * ov, self.d * ov if od is None else self.d * ov + self.v * od)
+
+  def __rmul__(self, o):
+    return Dual(o * self.v, o * self.d)
+
+  def __truediv__(self, o):
+    assert not isinstance(o, Dual)
+    return Dual(self.v / o, self.d / o)
+
+
+class NS(types.SimpleNamespace):
+  pass
+
+
+def consumer_namespace(state):
+  """Globals of the extracted reference code, with numpy stand-ins."""
+  others = {"jnp": np, "as_jax": np.asarray}
+  load_functions(os.path.join(MATH, "others.py"), ["_exprel"], others)
+
+  def exprel(x, threshold=None):  # brainpy.math.exprel: the float32 threshold 1e-5
+    x = np.asarray(x, np.float32)
+    return others["_exprel"](x, 1e-5 if threshold is None else threshold)
+
+  def vector_grad(func, argnums=0, return_value=False):
+    assert argnums == 0
+    def g(*args, **kw):
+      x = np.asarray(args[0], np.float32)
+      r = func(Dual(x, np.ones_like(x)), *args[1:], **kw)
+      grad, val = (r.d, r.v) if isinstance(r, Dual) else (np.zeros_like(x), np.asarray(r, np.float32))
+      return (grad, val) if return_value else grad
+    return g
+
+  class TrainingMode:
+    pass
+
+  class BatchingMode:
+    pass
+
+  bm = NS(where=np.where, logical_or=np.logical_or, exprel=exprel, vector_grad=vector_grad,
+          TrainingMode=TrainingMode, BatchingMode=BatchingMode,
+          as_jax=lambda x, dtype=None: np.asarray(x, dtype=dtype))
+
+  class Share:
+    def load(self, key):
+      return state[key]
+
+    def __getitem__(self, key):
+      return state[key]
+
+  def get_args(f):  # integrators/utils.py:30-100: variables before `t`, the rest after it
+    names = list(inspect.signature(f).parameters)
+    k = names.index("t")
+    return names[:k], names[k:], names
+
+  ns = {"np": np, "bm": bm, "share": Share(), "jnp": np, "jax": NS(lax=NS(stop_gradient=lambda x: x)),
+        "utils": NS(get_args=get_args), "joint_eq": NS(JointEq=type("JointEq", (), {})),
+        "errors": NS(DiffEqError=ValueError), "C": NS(DT="dt", multi_vars_msg="{cls}{vars}{eq}"),
+        "check": NS(is_checking=lambda: False), "jit_error": lambda *a, **k: None,
+        "ROTATE_UPDATE": "rotation", "CONCAT_UPDATE": "concat", "isinstance": isinstance}
+  return ns
+
+
+def make_consumer_classes(ns):
+  # exponential Euler (integrators/ode/exponential.py:338-364): the reference's integral
+  fn = load_method(os.path.join(DYN, "integrators", "ode", "exponential.py"), "ExponentialEuler", "_build_integrator")
+  exec(compile(ast.fix_missing_locations(ast.Module(body=[fn], type_ignores=[])), "exponential.py", "exec"), ns)
+  build_integrator = ns["_build_integrator"]
+
+  def odeint(f, dt):
+    (integral, vars_, pars_), = build_integrator(NS(dt=dt), f)
+    names = vars_ + pars_ + ["dt"]
+    def integral_func(*args):  # ExponentialEuler.build's mapping of positional arguments
+      kw = {names[i]: a for i, a in enumerate(args)}
+      return integral(kw[names[0]], **{a: kw[a] for a in names[1:] if a in kw})
+    return integral_func
+
+  class Var:
+    """bm.Variable stand-in: .value, in-place +=, and arithmetic on its value."""
+    def __init__(self, value):
+      self.value = value
+
+    def __iadd__(self, x):  # Variable += x
+      self.value = self.value + x
+      return self
+
+    def __array__(self, dtype=None, copy=None):
+      return np.asarray(self.value, dtype=dtype)
+
+  for op in ("add", "sub", "mul", "truediv", "le", "lt", "ge", "gt"):
+    for name in (f"__{op}__", f"__r{op}__"):
+      if hasattr(np.ndarray, name):
+        setattr(Var, name, (lambda nm: lambda self, o: getattr(np.asarray(self.value), nm)(o))(name))
+  Var.__neg__ = lambda self: -np.asarray(self.value)
+
+  class NeuBase:  # the mixin's current and delta input sums (mixin.py:427-469)
+    pass
+
+  load_class(os.path.join(DYN, "mixin.py"), "SupportInputProj", ["sum_current_inputs", "sum_delta_inputs"], [], ns)
+  ns["NeuBase"] = ns["SupportInputProj"]
+  lif = os.path.join(DYN, "dyn", "neurons", "lif.py")
+  load_class(lif, "LifLTC", ["derivative"], ["NeuBase"], ns)
+  load_class(lif, "LifRefLTC", ["update"], ["LifLTC"], ns)
+  load_class(lif, "LifRef", ["derivative", "update"], ["LifRefLTC"], ns)
+  load_class(os.path.join(DYN, "dyn", "synapses", "abstract_models.py"), "Expon", ["derivative", "update", "add_current"],
+             [], ns)
+  load_class(os.path.join(DYN, "dyn", "outs", "outputs.py"), "COBA", ["update"], [], ns)
+  load_class(os.path.join(DYN, "delay.py"), "VarDelay", ["retrieve", "update", "at"], [], ns)
+  return odeint, Var
+
+
+def consumer_net(ns, odeint, Var, n_exc, n_inh, ind_e, ptr_e, ind_i, ptr_i, we, wi, V0, ltc, d_e, d_i, steps,
+                 trace_steps, dt=0.1, inp=20.0):
+  """EICOBA_PostAlign (examples/dynamics_simulation/COBA.py:58-109) stepped with the
+  reference's own update methods; the projections' products are exact counts times the weight
+  (the operators are pinned by their own fixtures)."""
+  n = n_exc + n_inh
+  state = ns["share"].load.__self__ if False else None
+  groups = {}
+  for name, lo, hi in (("E", 0, n_exc), ("I", n_exc, n)):
+    cls = ns["LifRefLTC"] if ltc else ns["LifRef"]
+    neu = cls.__new__(cls)
+    neu.V_rest, neu.V_th, neu.V_reset, neu.tau, neu.tau_ref, neu.R = -60.0, -50.0, -60.0, 20.0, 5.0, 1.0
+    neu.V = Var(V0[lo:hi].astype(np.float32))
+    neu.spike = Var(np.zeros(hi - lo, bool))
+    neu.t_last_spike = Var(np.full(hi - lo, -1e7, np.float32))
+    neu.ref_var = False
+    neu.mode = None
+    neu.delta_inputs = {}
+    neu.integral = odeint(neu.derivative, dt)
+    syn = {}
+    for kind, tau, E in (("e", 5.0, 0.0), ("i", 10.0, -80.0)):
+      s = ns["Expon"].__new__(ns["Expon"])
+      s.tau = tau
+      s.g = Var(np.zeros(hi - lo, np.float32))
+      s.integral = odeint(s.derivative, dt)
+      o = ns["COBA"].__new__(ns["COBA"])
+      o.E = E
+      syn[kind] = (s, o)
+    # current inputs in registration order (E2E / E2I before I2E / I2I): excitatory first
+    neu.current_inputs = {k: (lambda V, s=s, o=o: o.update(s.g.value, V)) for k, (s, o) in syn.items()}
+    groups[name] = (neu, syn, lo, hi)
+  delays = {}
+  for name, d, lo, hi in (("E", d_e, 0, n_exc), ("I", d_i, n_exc, n)):
+    if d > 0:
+      dl = ns["VarDelay"].__new__(ns["VarDelay"])
+      dl.method, dl.max_length, dl.mode = "rotation", d, None
+      dl.data = np.zeros((d, hi - lo), bool)
+      dl.target = groups[name][0].spike
+      dl._registered_entries = {"proj": d}
+      delays[name] = dl
+
+  def spikes_of(name):
+    if name in delays:
+      return np.asarray(delays[name].at("proj"), bool)
+    return groups[name][0].spike.value
+
+  V_trace = np.zeros((trace_steps, n), np.float32)
+  counts = np.zeros(steps, np.int64)
+  for i in range(steps):
+    SHARE.update(i=i, t=np.float32(i) * np.float32(dt), dt=dt)
+    # projections (update order E2I, I2I, I2E, E2E): g += count * w, per post group
+    dge = np.zeros(n, np.float32)
+    dgi = np.zeros(n, np.float32)
+    for pre, ind, ptr, w, acc in (("E", ind_e, ptr_e, we, dge), ("I", ind_i, ptr_i, wi, dgi)):
+      act = np.nonzero(spikes_of(pre))[0]
+      cnt = np.zeros(n, np.int64)
+      for r in act:
+        np.add.at(cnt, ind[ptr[r]:ptr[r + 1]], 1)
+      acc += cnt.astype(np.float32) * np.float32(w)
+    for name, (neu, syn, lo, hi) in groups.items():
+      syn["e"][0].add_current(dge[lo:hi])
+      syn["i"][0].add_current(dgi[lo:hi])
+    # each group: its synapses decay (before-updates), then the neurons integrate
+    for name, (neu, syn, lo, hi) in groups.items():
+      syn["e"][0].update()
+      syn["i"][0].update()
+      neu.update(np.float32(inp))
+    for name, dl in delays.items():
+      dl.update()
+    V = np.concatenate([groups["E"][0].V.value, groups["I"][0].V.value])
+    sp = np.concatenate([groups["E"][0].spike.value, groups["I"][0].spike.value])
+    counts[i] = int(sp.sum())
+    if i < trace_steps:
+      V_trace[i] = V
+  return V_trace, counts
+
+
+SHARE = {}
+
+
+def gen_consumer():
+  global SHARE
+  ns = consumer_namespace(SHARE)
+  odeint, Var = make_consumer_classes(ns)
+  rng = np.random.default_rng(2024)
+  n_exc, n_inh = 160, 40
+  n = n_exc + n_inh
+  out = {}
+
+  def fixed_rows(m, K):
+    ptr = np.arange(0, m * K + 1, K, dtype=np.int32)
+    ind = np.concatenate([rng.choice(n, K, replace=False) for _ in range(m)]).astype(np.int32)
+    return ind, ptr
+
+  ind_e, ptr_e = fixed_rows(n_exc, 10)
+  ind_i, ptr_i = fixed_rows(n_inh, 10)
+  V0 = rng.normal(-55.0, 5.0, n).astype(np.float32)
+  out.update(ind_e=ind_e, ptr_e=ptr_e, ind_i=ind_i, ptr_i=ptr_i, V0=V0,
+             sizes=np.array([n_exc, n_inh], np.int64), weights=np.array([0.6, 6.7], np.float32))
+  for tag, ltc, de, di in (("ltc", True, 0, 0), ("lifref", False, 0, 0), ("ltc_d3_1", True, 3, 1), ("ltc_d2_0", True, 2, 0)):
+    Vt, counts = consumer_net(ns, odeint, Var, n_exc, n_inh, ind_e, ptr_e, ind_i, ptr_i, 0.6, 6.7, V0, ltc, de, di,
+                              steps=300, trace_steps=100)
+    out[f"{tag}|V"] = Vt
+    out[f"{tag}|counts"] = counts
+    out[f"{tag}|cfg"] = np.array([int(ltc), de, di], np.int64)
+  # VarDelay's rotating indices alone: what step's value each delay reads at each step
+  for L in (1, 3, 5):
+    for d in range(1, L + 1):
+      dl = ns["VarDelay"].__new__(ns["VarDelay"])
+      dl.method, dl.max_length, dl.mode = "rotation", L, None
+      dl.data = np.full((L, 1), -1, np.int64)
+      dl.target = Var(np.zeros(1, np.int64))
+      dl._registered_entries = {"x": d}
+      read = []
+      for i in range(24):
+        SHARE.update(i=i)
+        read.append(int(np.asarray(dl.at("x"))[0]))
+        dl.target.value = np.array([i], np.int64)  # the value step i produces
+        dl.update()
+      out[f"delay|L{L}|d{d}"] = np.array(read, np.int64)
+  return out
+
+
 def main():
   np.seterr(over="ignore")
   pl = gen_plasticity()
@@ -446,6 +754,9 @@ def main():
   np.savez_compressed(os.path.join(HERE, "jitconn.npz"), **jc)
   n_conn = sum(v.size for k, v in jc.items() if k.endswith("|rows"))
   print("jitconn:", len(jc), "arrays,", n_conn, "connections")
+  co = gen_consumer()
+  np.savez_compressed(os.path.join(HERE, "consumer.npz"), **co)
+  print("consumer:", len(co), "arrays")
 
 
 if __name__ == "__main__":

@@ -139,3 +139,29 @@ def test_delays_ops_and_graph_match_cluster(dyn):
   assert torch.equal(a.ring, b.ring) and torch.equal(a.ring, c.ring)
   with pytest.raises(ValueError):
     a.run(10, dt=0.05)
+
+
+def test_spike_ring_reads_as_reference_delay(bplib):
+  """The device's spike history (bp_spike_ring_record / bp_spike_ring_read) reads, at every
+  step, what the reference's VarDelay reads (tests/golden/consumer.npz, generated by
+  executing VarDelay.at / .retrieve / .update of brainpy/_src/delay.py): 8 neurons spike the
+  bits of step + 1, so a read decodes to the step it came from (0: nothing recorded yet)."""
+  import ctypes
+  from golden_util import load
+  from brainpy_gb300 import _lib
+  L = _lib.lib()
+  cons = load("consumer")
+  st = _lib.stream_handle()
+  for key in [k for k in cons.files if k.startswith("delay|")]:
+    _, ring_len, d = key.split("|")
+    ring_len, d = int(ring_len[1:]), int(d[1:])
+    want = cons[key]
+    ring = torch.zeros(ring_len, dtype=torch.int32, device="cuda")  # [ring_len][ceil(8 / 32)] words
+    out = torch.empty(8, dtype=torch.uint8, device="cuda")
+    for T in range(want.shape[0]):
+      _lib.check(L.bp_spike_ring_read(_lib.ptr(ring), ring_len, 8, 0, 8, d, T, None, _lib.ptr(out), st), "ring_read")
+      bits = out.cpu().numpy()
+      got = int(sum(int(b != 0) << j for j, b in enumerate(bits))) - 1
+      assert got == int(want[T]), (key, T, got, int(want[T]))
+      sp = torch.tensor([((T + 1) >> j) & 1 for j in range(8)], dtype=torch.uint8, device="cuda")
+      _lib.check(L.bp_spike_ring_record(_lib.ptr(sp), 8, _lib.ptr(ring), ring_len, T, None, st), "ring_record")

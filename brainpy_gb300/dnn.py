@@ -8,7 +8,9 @@ shape (pre_num, post_num) and transpose=True by default; just-in-time layers use
 shape=(num_out, num_in) and outdim_parallel = not atomic.  Inputs of more than one dimension
 are treated as a batch of vectors along the last axis (one launch pair for a planned CSR
 product).  Weights given as tensors that require a gradient are trained through the operators'
-differentiation rules; sharding and synaptic plasticity are not part of this package.
+differentiation rules.  The CSR layers' STDP updates (`stdp_update`, `csr_on_pre_update`,
+`csc_on_post_update`, linear.py:517-543 and :650-698) are here; sharding is not part of this
+package.
 """
 from typing import Optional
 

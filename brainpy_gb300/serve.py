@@ -58,7 +58,12 @@ class Job:
 
 
 def job_memory(job: Job) -> int:
-  """Device bytes a job holds while admitted (CSR: indices, indptr, tiled plan; state)."""
+  """Device bytes a job holds while admitted: its state (V, ge, gi, t_last in float32 and the
+  spike byte of every neuron, one spike count per step); for a CSR job also the int32 indices
+  and indptr, one tiled plan (segment offsets, 4 bytes per row and tile boundary, and 2 bytes
+  per padded entry: the cluster runner's plan of 4096-column tiles, or the per-operator path's
+  two projection plans, which together cover the same rows) and the per-operator path's event
+  workspace (the active-row lists of the rows); a jitconn job stores no matrix."""
   n = job.n
   state = n * (4 * 4 + 1) + 4 * int(job.duration_ms / 0.1 + 1)
   if job.conn == "jitconn":
@@ -67,7 +72,8 @@ def job_memory(job: Job) -> int:
   nnz = n * k
   tiles = math.ceil(n / 4096) if n <= 16 * 4096 else max(1, math.ceil(n / 27840))
   plan = 4 * n * (tiles + 1) + 2 * (nnz + (8 * tiles + 8) * n + 8)
-  return state + 4 * nnz + 4 * (n + 1) + plan + 2 * plan
+  lists = 4 * (math.ceil(n / 4096) * 4096 + math.ceil(n / 4096)) + 1024
+  return state + 4 * nnz + 4 * (n + 1) + plan + lists
 
 
 def build_job(job: Job, device) -> dyn.EINetwork:

@@ -283,6 +283,9 @@ bp_status bp_csrmv_planned_batch(const bp_csr_plan* plan, const float* w_homo, c
  * m with transpose=1 returns BP_ENOMEM).  All calls on a device share that array: calls
  * whose GPU work overlaps race, so order them on one stream.  The first call on each
  * device looks the array up (cudaGetSymbolAddress); make it before any stream capture.
+ * The address is kept per device ordinal for the life of the process: after a
+ * cudaDeviceReset (or with another context on the device) it is stale, so do not call this
+ * entry point across a device reset.
  * ------------------------------------------------------------------------- */
 int64_t bp_event_csrmv_noalloc_max_rows(void);
 bp_status bp_event_csrmv_noalloc(const float* data, int64_t ndata, const void* indices, const void* indptr,

@@ -33,23 +33,30 @@ def _workload(n, k, seed):
   return ind, ptr, heter, [bernoulli_events(n, r, seed=seed + 2 + j) for j, r in enumerate((0.02, 0.1))]
 
 
-def _with_workspace(L, data, ind, ptr, ev, n, transpose):
+def _events(ev, etype):
+  """bool events, or float32 events of both signs (the > 0 and != 0 rules then differ)."""
   from brainpy_gb300 import _lib
+  if etype == _lib.BP_EV_BOOL:
+    return ev.view(torch.uint8)
+  sign = torch.where(torch.arange(ev.numel(), device=ev.device) % 3 == 0, -1.0, 1.0)
+  return ev.to(torch.float32) * sign
+
+
+def _with_workspace(L, data, ind, ptr, ev, n, transpose, etype=0, itype=0):
   out = torch.full((n,), float("nan"), device="cuda")
   ws_bytes = L.bp_event_csrmv_workspace_size(n, n, transpose)
   ws = torch.empty(max(ws_bytes, 1), dtype=torch.uint8, device="cuda")
-  st = L.bp_event_csrmv(_vp(data), data.numel(), _vp(ind), _vp(ptr), _lib.BP_I32, ind.numel(),
-                        _vp(ev.view(torch.uint8)), _lib.BP_EV_BOOL, n, n, transpose, _vp(out), _vp(ws), ws_bytes,
+  st = L.bp_event_csrmv(_vp(data), data.numel(), _vp(ind), _vp(ptr), itype, ind.numel(),
+                        _vp(ev), etype, n, n, transpose, _vp(out), _vp(ws), ws_bytes,
                         ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
   assert st == 0, L.bp_last_error()
   return out
 
 
-def _no_alloc(L, data, ind, ptr, ev, n, transpose):
-  from brainpy_gb300 import _lib
+def _no_alloc(L, data, ind, ptr, ev, n, transpose, etype=0, itype=0):
   out = torch.full((n,), float("nan"), device="cuda")
-  st = L.bp_event_csrmv_noalloc(_vp(data), data.numel(), _vp(ind), _vp(ptr), _lib.BP_I32, ind.numel(),
-                                _vp(ev.view(torch.uint8)), _lib.BP_EV_BOOL, n, n, transpose, _vp(out),
+  st = L.bp_event_csrmv_noalloc(_vp(data), data.numel(), _vp(ind), _vp(ptr), itype, ind.numel(),
+                                _vp(ev), etype, n, n, transpose, _vp(out),
                                 ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
   assert st == 0, L.bp_last_error()
   return out
@@ -61,19 +68,24 @@ def _scaled_err(y, ref, terms):
   return float(np.max(np.abs(y - ref) / np.maximum(scale, 1e-30)))
 
 
-def test_matches_workspace_entry_point_twice(L):
+@pytest.mark.parametrize("etype", [0, 1, 2])  # BP_EV_BOOL, BP_EV_F32_POS, BP_EV_F32_NZ
+@pytest.mark.parametrize("itype", [0, 1])      # BP_I32, BP_I64
+def test_matches_workspace_entry_point_twice(L, etype, itype):
   n, k = 20000, 100
   ind, ptr, heter, spikes = _workload(n, k, seed=11)
+  if itype == 1:
+    ind, ptr = ind.to(torch.int64), ptr.to(torch.int64)
   homo = torch.tensor([0.6], device="cuda")
   for transpose in (1, 0):
     for ev in spikes:  # two calls in a row on different events
-      a = _no_alloc(L, homo, ind, ptr, ev, n, transpose)
-      b = _with_workspace(L, homo, ind, ptr, ev, n, transpose)
+      e = _events(ev, etype)
+      a = _no_alloc(L, homo, ind, ptr, e, n, transpose, etype, itype)
+      b = _with_workspace(L, homo, ind, ptr, e, n, transpose, etype, itype)
       torch.cuda.synchronize()
       assert torch.equal(a, b)
-      a = _no_alloc(L, heter, ind, ptr, ev, n, transpose)
-      b = _with_workspace(L, heter, ind, ptr, ev, n, transpose)
-      terms = _with_workspace(L, heter.abs(), ind, ptr, ev, n, transpose)
+      a = _no_alloc(L, heter, ind, ptr, e, n, transpose, etype, itype)
+      b = _with_workspace(L, heter, ind, ptr, e, n, transpose, etype, itype)
+      terms = _with_workspace(L, heter.abs(), ind, ptr, e, n, transpose, etype, itype)
       torch.cuda.synchronize()
       assert _scaled_err(a, b, terms) < 1e-5
 

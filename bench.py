@@ -56,6 +56,9 @@ def parse():
   ap.add_argument("--delay", type=float, default=None,
                   help="coba: synaptic delay (ms) of every projection, as FullProjAlignPostMg(delay=...)")
   ap.add_argument("--sim-steps", type=int, default=0, help="override the workload's number of steps")
+  ap.add_argument("--no-forms", action="store_true",
+                  help="event_csrmv: skip the batched / served / COBA-example forms reported beside the headline")
+  ap.add_argument("--serve-jobs", type=int, default=120, help="jobs of the served stream reported beside the headline")
   return ap.parse_args()
 
 
@@ -160,6 +163,14 @@ def alg_bytes(n, active, k, heter):
   return n + 8 * active + 4 * e + (4 * e if heter else 0) + 4 * n
 
 
+def headline_config(args, ws=1):
+  return {"workload": f"event_csrmv_T N={args.n} K={args.fanout} r={args.rate} {args.weights}",
+          "n": args.n, "fanout": args.fanout, "rate": args.rate, "weights": args.weights, "index": "int32",
+          "l2": "inputs larger than L2: 8 rotating spike vectors whose segments (8 x ~54 MB) exceed "
+                "the 126 MB L2; calls back to back",
+          "parallelism": f"replicas x{ws}"}
+
+
 def run_cpu_baseline(args, data, ind, ptr, spikes, seconds):
   """The reference's CPU path for this operator timed on the host cores: its serial njit
   transpose loop (restated in C), run as independent calls on every host thread at once
@@ -201,7 +212,7 @@ def run_reference(args):
   line = {"impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": UNIT, "n_gpus": args.gpus,
           "steps": steps, "warmup": warm, "ms_per_step": None, "higher_is_better": True,
           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-          "config": {"workload": f"event_csrmv_T N={args.n} K={args.fanout} r={args.rate} {args.weights}"},
+          "config": headline_config(args, args.gpus),
           "cpu_baseline": cpu,
           "e2e": {"value": cpu["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
   mean_events = float(np.mean([int(s.sum()) for s in spikes])) * args.fanout
@@ -272,8 +283,24 @@ def main():
   e1.record()
   torch.cuda.synchronize()
   t_wall = time.perf_counter() - t_wall
-  clk = clocks.stop()
   step_ms = e0.elapsed_time(e1) / args.steps
+  # sustained window: the same graph replayed for about a second, each replay timed on its own;
+  # the clock sampler runs across both the timed replay and this window
+  sus = []
+  t_sus = time.perf_counter()
+  while time.perf_counter() - t_sus < 1.0 or len(sus) < 20:
+    a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a_.record()
+    g_run.replay()
+    b_.record()
+    sus.append((a_, b_))
+    if len(sus) % 50 == 0:
+      b_.synchronize()
+  torch.cuda.synchronize()
+  clk = clocks.stop()
+  sus_ms = sorted(a_.elapsed_time(b_) / args.steps for a_, b_ in sus)
+  sustained = {"ms_per_step_median": sus_ms[len(sus_ms) // 2], "ms_per_step_min": sus_ms[0],
+               "ms_per_step_max": sus_ms[-1], "replays": len(sus_ms), "calls_per_replay": args.steps}
   events_done = sum(active[i % nv] for i in range(args.steps)) * k
   # the graphed results equal eager calls on the same spikes
   heter = args.weights == "heter"
@@ -380,21 +407,67 @@ def main():
   line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
           "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
           "dtype": "f32", "data": "synthetic",
-          "config": {"workload": f"event_csrmv_T N={n} K={k} r={args.rate} {args.weights}",
-                     "n": n, "fanout": k, "rate": args.rate, "weights": args.weights, "index": "int32",
-                     "l2": "inputs larger than L2: 8 rotating spike vectors whose segments (8 x ~54 MB) exceed "
-                           "the 126 MB L2; calls back to back",
-                     "parallelism": f"replicas x{ws}"},
+          "config": headline_config(args, ws),
           "roofline": roof, "e2e": e2e, "gpu_launches": None, "clocks": clk,
-          "cold_l2_ms_per_call": cold_ms,
+          "cold_l2_ms_per_call": cold_ms, "sustained": sustained,
           "wall_s_timed_loop": t_wall}
   line["gpu_launches"] = args.steps * launches_per_step(args)
   if rank == 0 and ws == 1 and not args.no_cpu_baseline:
     line["cpu_baseline"] = run_cpu_baseline(args, data, ind, ptr, spikes, args.cpu_seconds)
+  if rank == 0 and ws == 1 and not args.no_forms:
+    del data, ind, ptr, spikes, outs, g_run, g_warm, g_e2e, keep, singles
+    event.release_plans()
+    torch.cuda.empty_cache()
+    line["north_star_forms"] = north_star_forms(args)
   if rank == 0:
     print(json.dumps(line))
   if ws > 1:
     torch.distributed.destroy_process_group()
+
+
+def north_star_forms(args):
+  """The batched and served forms and the COBA example, each timed with CUDA events under its
+  own clock record, summarised beside the headline operator line."""
+  import copy
+  out = {}
+  a = copy.copy(args)
+  a.sim_steps = 0
+  a.delay = None
+  r = bench_coba(a)
+  out["coba_example"] = {
+      "config": r["config"]["workload"], "runner_steps_per_s": r["value"], "ms_per_step": r["ms_per_step"],
+      "per_op_path_steps_per_s": r["per_op_path_steps_per_s"],
+      "per_op_graph_steps_per_s": r["per_op_graph_steps_per_s"],
+      "cpu_oracle_steps_per_s": r["cpu_baseline"]["value"], "cpu_cores": r["cpu_baseline"]["cores"],
+      "runner_vs_per_op": r["value"] / r["per_op_path_steps_per_s"],
+      "runner_vs_cpu": r["value"] / r["cpu_baseline"]["value"],
+      "firing_rate_hz": r["firing_rate_hz"], "e2e_steps_per_s": r["e2e"]["value"], "clocks": r["clocks"]}
+  torch.cuda.empty_cache()
+  a = copy.copy(args)
+  a.sim_steps = 0
+  a.nets = 256
+  r = bench_batched(a)
+  out["batched_sweep"] = {
+      "config": r["config"]["workload"], "network_steps_per_s": r["value"],
+      "plain_network_steps_per_s": r["plain_per_network_path"]["value"],
+      "plain_sample": r["plain_per_network_path"]["sample"], "speedup_vs_plain": r["speedup_vs_plain"],
+      "synaptic_events_per_s": r["synaptic_events_per_s"], "accuracy": r["accuracy"],
+      "launches": r["gpu_launches"], "clocks": r["clocks"]}
+  torch.cuda.empty_cache()
+  from brainpy_gb300 import serve
+  a = copy.copy(args)
+  a.nets = args.serve_jobs
+  clocks = ClockSampler(torch.cuda.current_device())
+  r = serve.bench(a)
+  clk = clocks.stop()
+  out["served_stream"] = {
+      "config": r["config"]["workload"], "jobs": r["jobs_done"], "p50_s": r["p50_s"], "p99_s": r["p99_s"],
+      "wall_s": r["wall_s"], "network_steps_per_s": r["network_steps_per_s"],
+      "synaptic_events_per_s": r["synaptic_events_per_s"],
+      "plain_network_steps_per_s": r["plain_per_network_path"]["value"],
+      "plain_sample": r["plain_per_network_path"]["sample"], "speedup_vs_plain": r["speedup_vs_plain"],
+      "clocks": clk}
+  return out
 
 
 # ---------------------------------------------------------------------------------------

@@ -181,6 +181,87 @@ __device__ __forceinline__ bool event_at(const void* events, int64_t i) {
   return ev_on_f32(__ldg(static_cast<const float*>(events) + i), ET);
 }
 
+// transpose=1 on a small matrix, in one launch: a single CTA keeps the n output columns as
+// shared-memory accumulators, compacts a round of events into a shared row list, scatters
+// the listed rows (one warp per row, up to 128 entries per load round) and finally writes
+// count * w (or the float sums) once.  No global atomics, no memsets, no second kernel:
+// at the sizes of a 4000-neuron network the launches, not the bytes, are the cost of the
+// general path.  Same arithmetic as the general path (exact uint32 counts for homogeneous
+// weights, float32 sums otherwise).
+constexpr int kSmallThreads = 1024;
+constexpr int kSmallRound = kSmallThreads * 4;  // events examined per round (4 per thread)
+constexpr int64_t kSmallMaxN = 49152;           // output words in shared memory (192 KB)
+constexpr int64_t kSmallMaxM = 32768;           // at most 8 rounds of event scanning
+constexpr int64_t kSmallMaxNnz = 1 << 19;       // worst case (every row active): 2^19 shared adds
+
+static size_t small_smem_bytes(int64_t n) { return sizeof(uint32_t) * ((size_t)n + kSmallRound + 1); }
+
+template <typename IdxT, bool HOMO, int ET>
+__global__ void __launch_bounds__(kSmallThreads) ecsr_t_small_kernel(const IdxT* __restrict__ indptr,
+                                                                     const IdxT* __restrict__ indices,
+                                                                     const float* __restrict__ data, int64_t nnz,
+                                                                     int64_t m, int64_t n,
+                                                                     const void* __restrict__ events,
+                                                                     float* __restrict__ out) {
+  extern __shared__ uint32_t sm_small[];
+  uint32_t* acc = sm_small;                          // n words
+  int32_t* rows = reinterpret_cast<int32_t*>(sm_small + n);  // kSmallRound row ids
+  int32_t* n_rows = rows + kSmallRound;
+  const int lane = lane_id(), warp = threadIdx.x >> 5;
+  constexpr int kWarps = kSmallThreads / 32;
+  for (int64_t i = threadIdx.x; i < n; i += kSmallThreads) acc[i] = 0u;
+  for (int64_t r0 = 0; r0 < m; r0 += kSmallRound) {
+    if (threadIdx.x == 0) *n_rows = 0;
+    __syncthreads();  // accumulators zeroed / previous round's list consumed
+    bool on[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t r = r0 + u * kSmallThreads + threadIdx.x;
+      on[u] = r < m && event_at<ET>(events, r);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const unsigned act = __ballot_sync(0xffffffffu, on[u]);
+      if (!act) continue;
+      int base = 0;
+      if (lane == 0) base = atomicAdd(n_rows, __popc(act));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (on[u]) rows[base + __popc(act & ((1u << lane) - 1u))] = (int32_t)(r0 + u * kSmallThreads + threadIdx.x);
+    }
+    __syncthreads();
+    const int cnt = *n_rows;
+    for (int a = warp; a < cnt; a += kWarps) {
+      int64_t b, e;
+      row_bounds(indptr, (int64_t)rows[a], nnz, b, e);
+      for (int64_t j0 = b; j0 < e; j0 += 128) {
+        int64_t c[4];
+        float w[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int64_t j = j0 + lane + 32 * u;
+          c[u] = j < e ? (int64_t)indices[j] : -1;
+          if (!HOMO) w[u] = j < e ? data[j] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          if ((uint64_t)c[u] < (uint64_t)n) {
+            if (HOMO) atomicAdd(acc + c[u], 1u);
+            else atomicAdd(reinterpret_cast<float*>(acc) + c[u], w[u]);
+          }
+        }
+      }
+    }
+    __syncthreads();  // the list is reused by the next round
+  }
+  if (m <= 0) __syncthreads();
+  if (HOMO) {
+    const float w0 = data[0];
+    for (int64_t i = threadIdx.x; i < n; i += kSmallThreads) out[i] = (float)acc[i] * w0;
+  } else {
+    for (int64_t i = threadIdx.x; i < n; i += kSmallThreads) out[i] = __uint_as_float(acc[i]);
+  }
+}
+
 // transpose=0, one warp per row.
 template <typename IdxT, bool HOMO, int ET>
 __global__ void __launch_bounds__(256) ecsr_n_kernel(const IdxT* __restrict__ indptr,
@@ -306,10 +387,54 @@ bp_status compact_events(const void* events, bp_etype et, int64_t m, int32_t* li
   return BP_EINVAL;
 }
 
+template <typename IdxT, bool HOMO, int ET>
+static bp_status launch_t_small(const IdxT* indptr, const IdxT* indices, const float* data, int64_t nnz, int64_t m,
+                                int64_t n, const void* events, float* out, cudaStream_t st) {
+  auto kfn = ecsr_t_small_kernel<IdxT, HOMO, ET>;
+  const size_t smem = small_smem_bytes(n);
+  if (smem > 48 * 1024) {
+    static bool configured[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) dev = 0;
+    if (!configured[dev]) {
+      BP_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)small_smem_bytes(kSmallMaxN)));
+      configured[dev] = true;
+    }
+  }
+  {
+    ScopedKernelTimer tk(st);
+    kfn<<<1, kSmallThreads, smem, st>>>(indptr, indices, data, nnz, m, n, events, out);
+  }
+  return check_launch("ecsr_t_small_kernel");
+}
+
+template <typename IdxT, bool HOMO>
+static bp_status ecsr_t_small(const IdxT* indptr, const IdxT* indices, const float* data, int64_t nnz, int64_t m,
+                              int64_t n, const void* events, bp_etype et, float* out, cudaStream_t st) {
+  switch (et) {
+    case BP_EV_BOOL: return launch_t_small<IdxT, HOMO, BP_EV_BOOL>(indptr, indices, data, nnz, m, n, events, out, st);
+    case BP_EV_F32_POS:
+      return launch_t_small<IdxT, HOMO, BP_EV_F32_POS>(indptr, indices, data, nnz, m, n, events, out, st);
+    case BP_EV_F32_NZ:
+      return launch_t_small<IdxT, HOMO, BP_EV_F32_NZ>(indptr, indices, data, nnz, m, n, events, out, st);
+  }
+  return BP_EINVAL;
+}
+
+// Whether a transposed product goes through the single-CTA kernel.
+static bool t_small_fits(int64_t m, int64_t n, int64_t nnz) {
+  return m <= kSmallMaxM && n <= kSmallMaxN && nnz <= kSmallMaxNnz;
+}
+
 template <typename IdxT>
 static bp_status ecsr_transpose_rowpar(const float* data, bool homo, const IdxT* indices, const IdxT* indptr,
                                        int64_t nnz, const void* events, bp_etype et, int64_t m, int64_t n,
                                        float* out, int32_t* list, int32_t* count, cudaStream_t st) {
+  if (t_small_fits(m, n, nnz))
+    return homo ? ecsr_t_small<IdxT, true>(indptr, indices, data, nnz, m, n, events, et, out, st)
+                : ecsr_t_small<IdxT, false>(indptr, indices, data, nnz, m, n, events, et, out, st);
   BP_CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(int32_t), st));
   BP_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * (size_t)n, st));
   bp_status s = compact_events(events, et, m, list, count, st);

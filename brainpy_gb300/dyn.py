@@ -121,6 +121,7 @@ class EINetwork:
     self.t_step = 0
     self._plan = None
     self._split = None
+    self._opc = None
     # delays in steps and the spike history: step T's spike bits in ring[T mod L]
     self.delay_dt = float(dt)
     self.d_e, self.d_i = delay_steps(delay_e, dt), delay_steps(delay_i, dt)
@@ -243,19 +244,52 @@ class EINetwork:
                                          _lib.stream_handle(self.device))
     _lib.check(st, "spike_ring_record")
 
+  def _csr_ops(self):
+    """Call state of the two event.csrmv projections of the per-operator path, built once.
+    For the excitatory-row and the inhibitory-row matrix: its weight as a device scalar, a
+    persistent output vector, and either the plan that event.csrmv runs on for this matrix
+    (large networks) or the argument list of a direct bp_event_csrmv call with its workspace
+    (small ones, where the library runs a single-launch kernel).  The checks and allocations
+    of the public call are done here once instead of every step; the result is the same."""
+    if self._opc is None:
+      n = self.n
+      L = _lib.lib()
+      ops = []
+      for (ind, ptr), m, w in zip(self._csr_split(), (self.n_exc, n - self.n_exc), (self.we, self.wi)):
+        wt = torch.full((1,), w, device=self.device)
+        out = torch.empty(n, device=self.device)
+        plan = _event._plan_for(wt, ind, ptr, (m, n))
+        ws, args = None, None
+        if plan is None:
+          wsb = int(L.bp_event_csrmv_workspace_size(m, n, 1))
+          ws = _lib.workspace(wsb, self.device)
+          itype = _lib.BP_I32 if ind.dtype == torch.int32 else _lib.BP_I64
+          args = (wt.data_ptr(), ind.data_ptr() if ind.numel() else 0, ptr.data_ptr(), itype, ind.numel(), m, n,
+                  out.data_ptr(), ws.data_ptr(), wsb)
+        ops.append((wt, out, plan, ws, args))
+      self._opc = ops
+    return self._opc
+
   def _propagate_ops(self, T=None):
     """Conductance increments of one step (per-operator path): the rows' spikes of the
     previous step, or of their group's delay before step T."""
     ne, n = self.n_exc, self.n
-    if not hasattr(self, "_w_t"):
-      self._w_t = (torch.full((1,), self.we, device=self.device), torch.full((1,), self.wi, device=self.device))
-    w_e, w_i = self._w_t
     se, si = (self.spike[:ne], self.spike[ne:]) if self.ring is None else self._delayed_spikes(T)
     if self.jitconn is None:
-      (ie, pe), (ii, pi) = self._csr_split()
-      dge = _event.csrmv(w_e, ie, pe, se, shape=(ne, n), transpose=True)
-      dgi = _event.csrmv(w_i, ii, pi, si, shape=(n - ne, n), transpose=True)
-      return dge, dgi
+      res = []
+      fn = None
+      for (wt, out, plan, _, args), ev in zip(self._csr_ops(), (se, si)):
+        if plan is not None:
+          res.append(plan.csrmv(ev, wt, out=out))
+          continue
+        if fn is None:
+          fn, sp = _lib.lib().bp_event_csrmv, _lib.raw_stream(self.device)
+        w, ix, ip, itype, nnz, m, nn, o, ws, wsb = args
+        st = fn(w, 1, ix, ip, itype, nnz, ev.data_ptr(), _lib.BP_EV_BOOL, m, nn, 1, o, ws, wsb, sp)
+        if st:
+          _lib.check(st, "event.csrmv")
+        res.append(out)
+      return res[0], res[1]
     p, s = self.jitconn["prob"], self.jitconn["seeds"]
     odp = bool(self.jitconn.get("outdim_parallel", True))
     ni = n - ne

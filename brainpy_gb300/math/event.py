@@ -350,6 +350,14 @@ def _cached_plan(data, indices, indptr, shape, force=False, routed=True, kind="g
   return plan
 
 
+def _plan_for(data, indices, indptr, shape):
+  """The plan the transposed event product of this matrix runs on (autotuned route first,
+  then the size thresholds), or None for the plain CSR kernels."""
+  route = _route(data, indices, indptr, shape)
+  return _cached_plan(data, indices, indptr, shape, force=route in ("tiled", "split"),
+                      kind=_plan_kind(data, shape[1], route))
+
+
 def _valid_choice(choice):
   if choice in ("row", "split"):
     return True
@@ -473,9 +481,7 @@ def _event_csrmv(data, indices, indptr, events, shape, transpose, float_rule, ou
   m, n = int(shape[0]), int(shape[1])
   n_out = n if transpose else m
   if transpose and use_plan:
-    route = _route(data, indices, indptr, (m, n))
-    plan = _cached_plan(data, indices, indptr, (m, n), force=route in ("tiled", "split"),
-                        kind=_plan_kind(data, n, route))
+    plan = _plan_for(data, indices, indptr, (m, n))
     if plan is not None:
       return plan.csrmv(events, None if plan.heter else data, out=out, float_rule=float_rule)
   if out is None:

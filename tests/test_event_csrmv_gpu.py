@@ -97,6 +97,33 @@ def test_edge_cases(ev, orc):
   assert y.shape == (9,) and float(y.abs().sum()) == 0.0
 
 
+@pytest.mark.parametrize("m,n,k", [
+    (3200, 4000, 80),     # the COBA example's excitatory rows: one round of the single-CTA kernel
+    (20000, 3000, 20),    # several rounds of event scanning (4096 events a round)
+    (5000, 49152, 100),   # the largest output held in shared memory
+    (5000, 49153, 100),   # one column more: the general path
+    (600, 4000, 900),     # 540K entries: above the single-launch entry limit
+])
+def test_small_single_launch_path(ev, orc, m, n, k):
+  """The single-launch kernel of small transposed products (shared-memory accumulators)
+  and the general path on either side of its limits agree with the oracle: bit-exact
+  counts for a homogeneous weight, the FP64 bar for heterogeneous weights, every event
+  rule and both index types."""
+  from brainpy_gb300.connect import fixed_prob_csr, normal_weights
+  ind, ptr = fixed_prob_csr(m, n, k, seed=4)
+  ind_h, ptr_h = ind.cpu().numpy(), ptr.cpu().numpy()
+  heter = normal_weights(ind.numel(), 0.5, 0.1, seed=5).cpu().numpy()
+  rng = np.random.default_rng(6)
+  for rate in (0.0, 0.02, 1.0):
+    events = rng.random(m) < rate
+    _check(ev, orc, np.float32(0.6), ind_h, ptr_h, events, (m, n), True)
+    _check(ev, orc, heter, ind_h, ptr_h, events, (m, n), True)
+  evf = rng.choice(np.array([0.0, 1.0, -1.0, 0.25], np.float32), m)
+  _check(ev, orc, np.float32(-1.5), ind_h, ptr_h, evf, (m, n), True)
+  _check(ev, orc, heter, ind_h, ptr_h, evf, (m, n), True, taichi=True)
+  _check(ev, orc, heter, ind_h.astype(np.int64), ptr_h.astype(np.int64), rng.random(m) < 0.1, (m, n), True)
+
+
 def test_shape_errors(ev):
   ind = torch.zeros(4, dtype=torch.int32, device="cuda")
   ptr = torch.tensor([0, 2, 4], dtype=torch.int32, device="cuda")

@@ -664,11 +664,75 @@ def _graph_time(fn, flush_buf, steps=20):
   return sum(a.elapsed_time(b) for a, b in ev) / steps * 1e-3
 
 
+def _event_time(fn, flush_buf, steps=20):
+  """Mean device time of fn() called eagerly (launch and set-up included), L2 flushed before
+  each call."""
+  for _ in range(3):
+    fn()
+  torch.cuda.synchronize()
+  ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+  for a, b in ev:
+    flush_buf.zero_()
+    a.record()
+    fn()
+    b.record()
+  torch.cuda.synchronize()
+  return sum(a.elapsed_time(b) for a, b in ev) / steps * 1e-3
+
+
+def _cusparse_points(ind, ptr, n, k, x, one, flush_buf, peak, ours):
+  """torch's CSR SpMV (cuSPARSE) on the same matrix, the homogeneous weight broadcast to every
+  entry as the reference's GPU method does (brainpy/_src/math/sparse/_csr_mv.py:197-208):
+  y = A x and y = A^T x (A^T as torch's CSC view of A).  Timed eagerly (torch's dispatch and
+  cuSPARSE's descriptor set-up are in every call), which matters only at the small sizes.
+  Each point carries our sparse.csrmv time on the same product and the largest difference."""
+  from brainpy_gb300.math import sparse
+  pts = []
+  vals = torch.ones(ind.numel(), device="cuda")
+  A = torch.sparse_csr_tensor(ptr, ind, vals, (n, n))
+  b = 4 * (n + 1) + 8 * ind.numel() + 8 * n
+  for T in (False, True):
+    M = A.t() if T else A
+    try:
+      y = torch.mv(M, x)
+      t = _event_time(lambda: torch.mv(M, x), flush_buf)
+    except (RuntimeError, NotImplementedError) as e:
+      pts.append({"op": "cusparse", "T": T, "n": n, "k": k, "unavailable": str(e).splitlines()[0][:160]})
+      continue
+    ref = sparse.csrmv(one, ind, ptr, x, shape=(n, n), transpose=T)
+    diff = float((y - ref).abs().max() / ref.abs().max().clamp_min(1e-30))
+    pts.append({"op": "cusparse", "impl": "torch.mv on a CSR tensor" + (" (CSC view)" if T else ""), "T": T,
+                "n": n, "k": k, "w": "homo broadcast to nnz", "us": t * 1e6, "nnz_per_s": ind.numel() / t,
+                "hbm_frac": b / t / 1e9 / peak, "timing": "eager, CUDA events",
+                "ours_us": ours[T] * 1e6, "ours_speedup": t / ours[T], "max_rel_diff": diff})
+    del y, ref
+  # A^T stored as its own CSR matrix (converted once, outside the timing): cuSPARSE's plain
+  # y = B x on B = A^T, the form a user of torch would keep for repeated transposed products
+  try:
+    B = A.t().to_sparse_csr()
+    y = torch.mv(B, x)
+    t = _event_time(lambda: torch.mv(B, x), flush_buf)
+    ref = sparse.csrmv(one, ind, ptr, x, shape=(n, n), transpose=True)
+    diff = float((y - ref).abs().max() / ref.abs().max().clamp_min(1e-30))
+    pts.append({"op": "cusparse", "impl": "torch.mv on A^T converted to CSR", "T": True, "n": n, "k": k,
+                "w": "homo broadcast to nnz", "us": t * 1e6, "nnz_per_s": ind.numel() / t,
+                "hbm_frac": b / t / 1e9 / peak, "timing": "eager, CUDA events", "ours_us": ours[True] * 1e6,
+                "ours_speedup": t / ours[True], "max_rel_diff": diff})
+    del B, y, ref
+  except (RuntimeError, NotImplementedError) as e:
+    pts.append({"op": "cusparse", "impl": "A^T converted to CSR", "T": True, "n": n, "k": k,
+                "unavailable": str(e).splitlines()[0][:160]})
+  del A, vals
+  torch.cuda.empty_cache()
+  return pts
+
+
 def bench_sweep(args):
   """The operator sweep: event.csrmv transpose=True on square FixedProb CSR, N in {1e4, 1e5,
   1e6}, K in {100, 1000}, rate in {0.5, 2, 10} %, homogeneous 1.0 / heterogeneous N(0.5, 0.1);
-  sparse.csrmv transpose=True on a dense N(0, 1) vector; jitconn event_mv_prob_{homo, uniform,
-  normal} with p = K/N, seed 42, both outdim_parallel.  One JSON line with every point."""
+  sparse.csrmv (both orientations) on a dense N(0, 1) vector beside torch's CSR SpMV (cuSPARSE)
+  on the same matrix; jitconn event_mv_prob_{homo, uniform, normal} with p = K/N, seed 42, both
+  outdim_parallel.  One JSON line with every point."""
   from brainpy_gb300.connect import bernoulli_events, fixed_prob_csr, normal_weights
   from brainpy_gb300.math import event, jitconn, sparse
   peak, _ = load_peaks()
@@ -688,10 +752,18 @@ def bench_sweep(args):
           pts.append({"op": "event.csrmv", "T": True, "n": n, "k": k, "rate": rate, "w": name, "us": t * 1e6,
                       "events_per_s": a * k / t, "hbm_frac": b / t / 1e9 / peak})
       x = torch.randn(n, device="cuda")
-      t = _graph_time(lambda: sparse.csrmv(one, ind, ptr, x, shape=(n, n), transpose=True), flush_buf)
       b = 4 * (n + 1) + 4 * ind.numel() + 8 * n
-      pts.append({"op": "sparse.csrmv", "T": True, "n": n, "k": k, "w": "homo", "us": t * 1e6,
-                  "nnz_per_s": ind.numel() / t, "hbm_frac": b / t / 1e9 / peak})
+      ours = {}
+      for T in (True, False):
+        ours[T] = _graph_time(lambda: sparse.csrmv(one, ind, ptr, x, shape=(n, n), transpose=T), flush_buf)
+        pts.append({"op": "sparse.csrmv", "T": T, "n": n, "k": k, "w": "homo", "us": ours[T] * 1e6,
+                    "nnz_per_s": ind.numel() / ours[T], "hbm_frac": b / ours[T] / 1e9 / peak})
+      from brainpy_gb300.math.sparse import _csrmv
+      for T in (True, False):  # the plain-CSR kernels of the same products (no plan)
+        t = _graph_time(lambda: _csrmv(one, ind, ptr, x, (n, n), T, use_plan=False), flush_buf)
+        pts.append({"op": "sparse.csrmv", "path": "plain CSR", "T": T, "n": n, "k": k, "w": "homo",
+                    "us": t * 1e6, "nnz_per_s": ind.numel() / t, "hbm_frac": b / t / 1e9 / peak})
+      pts += _cusparse_points(ind, ptr, n, k, x, one, flush_buf, peak, ours)
       del ind, ptr, wh
       torch.cuda.empty_cache()
       sp = bernoulli_events(n, 0.02, seed=2)

@@ -47,11 +47,22 @@ __global__ void __launch_bounds__(256) csrmv_n_kernel(const IdxT* __restrict__ i
         else acc = fmaf(data[j + 32 * u], xv[u], acc);
       }
     }
-    for (; j < e; j += 32) {
-      int64_t c = (int64_t)indices[j];
-      float xv = (uint64_t)c < (uint64_t)n ? __ldg(x + c) : 0.0f;
-      if (HOMO) acc += xv;
-      else acc = fmaf(data[j], xv, acc);
+    // the rest of the row (< 32 * kNUnroll entries): up to 4 entries per lane in flight a
+    // round, predicated, still summed in j order
+    for (; j < e; j += 32 * 4) {
+      int64_t c[4];
+      float xv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) c[u] = j + 32 * u < e ? (int64_t)indices[j + 32 * u] : -1;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) xv[u] = (uint64_t)c[u] < (uint64_t)n ? __ldg(x + c[u]) : 0.0f;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (j + 32 * u < e) {
+          if (HOMO) acc += xv[u];
+          else acc = fmaf(data[j + 32 * u], xv[u], acc);
+        }
+      }
     }
     if (HOMO) acc *= __ldg(data);
     acc = warp_sum(acc);

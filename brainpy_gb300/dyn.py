@@ -122,6 +122,7 @@ class EINetwork:
     self._plan = None
     self._split = None
     self._opc = None
+    self._pc = None
     # delays in steps and the spike history: step T's spike bits in ring[T mod L]
     self.delay_dt = float(dt)
     self.d_e, self.d_i = delay_steps(delay_e, dt), delay_steps(delay_i, dt)
@@ -306,12 +307,17 @@ class EINetwork:
     """One step through the per-operator path (propagation calls + neuron kernel)."""
     T = self.t_step if step_dev is None else _DevStep(step_dev, offset)
     dge, dgi = self._propagate_ops(T)
+    pc = self._pc if self._pc is not None else ctypes.byref(self.params.c())
     if step_dev is None:
-      lif_coba_step(self.params, self.V, self.ge, self.gi, self.t_last, self.spike, dge, dgi, self.t_step, dt)
+      st = _lib.lib().bp_lif_coba_step(pc, self.n, self.V.data_ptr(), self.ge.data_ptr(), self.gi.data_ptr(),
+                                       self.t_last.data_ptr(), self.spike.data_ptr(), dge.data_ptr(),
+                                       dgi.data_ptr(), int(self.t_step), float(dt), _lib.raw_stream(self.device))
+      if st:
+        _lib.check(st, "lif_coba_step")
       self._record_spikes(T)
       self.t_step += 1
       return
-    st = _lib.lib().bp_lif_coba_step_dev(ctypes.byref(self.params.c()), self.n, _lib.ptr(self.V), _lib.ptr(self.ge),
+    st = _lib.lib().bp_lif_coba_step_dev(pc, self.n, _lib.ptr(self.V), _lib.ptr(self.ge),
                                          _lib.ptr(self.gi), _lib.ptr(self.t_last),
                                          _lib.ptr(self.spike.view(torch.uint8)), _lib.ptr(dge), _lib.ptr(dgi),
                                          _lib.ptr(step_dev), int(offset), float(dt), _lib.stream_handle(self.device))
@@ -336,11 +342,18 @@ class EINetwork:
       self._run_ops_graph(steps, dt, counts, graph_steps)
       return counts, None
     trace = []
-    for s in range(steps):
-      self.step_ops(dt)
-      counts[s] = self.spike.sum()
-      if s < v_trace_steps:
-        trace.append(self.V.clone())
+    self._pc = ctypes.byref(self.params.c())  # the parameters stay fixed during a run
+    try:
+      for s in range(steps):
+        self.step_ops(dt)
+        if counts.dtype == torch.int32:
+          torch.sum(self.spike, 0, dtype=torch.int32, out=counts[s])
+        else:
+          counts[s] = self.spike.sum()
+        if s < v_trace_steps:
+          trace.append(self.V.clone())
+    finally:
+      self._pc = None
     return counts, (torch.stack(trace) if trace else None)
 
   def _run_ops_graph(self, steps, dt, counts, graph_steps):

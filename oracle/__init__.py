@@ -54,6 +54,7 @@ def lib():
         "orc_lfsr88_stream": (None, [_U32, _I32, _P]),
         "orc_jitconn_connections": (_I64, [_I32, _F32, _F32, _I32, _U32, _I64, _I64, _I32, _I32, _I64, _P, _P, _P]),
         "orc_jitconn_mv": (None, [_I32, _I32, _P, _I64, _I64, _F32, _F32, _I32, _U32, _I32, _I32, _P, _P]),
+        "orc_jitconn_mv_rows": (None, [_I32, _I32, _P, _I64, _I64, _F32, _F32, _I32, _U32, _I32, _P, _P, _P]),
         "orc_event_csrmv": (None, [_P, _I64, _P, _P, _I32, _P, _I32, _I64, _I64, _I32, _P, _P, _P, _P]),
         "orc_csrmv": (None, [_P, _I64, _P, _P, _I32, _P, _I64, _I64, _I32, _P, _P, _P]),
         "orc_event_info": (_I64, [_P, _I64, _P]),
@@ -129,6 +130,22 @@ def jitconn_mv(kind, vec, num_row, p0, p1, clen, seed, outdim_parallel, variant=
   lib().orc_jitconn_mv(KINDS[kind], vec_kind, _p(vec), num_row, vec.shape[0], p0, p1, clen, seed,
                        int(outdim_parallel), 0 if variant == "gpu" else 1, _p(out), _p(ab))
   return out, ab
+
+
+def jitconn_mv_rows(kind, vec, num_row, p0, p1, clen, seed, rows, variant="gpu", vec_kind=None):
+  """Pull form (outdim_parallel) of jitconn_mv for the output rows `rows` only: returns
+  (y64[rows], abs64[rows])."""
+  vec = np.ascontiguousarray(vec)
+  if vec_kind is None:
+    vec_kind = 0 if vec.dtype == np.bool_ else 2
+  vec = vec.view(np.uint8) if vec.dtype == np.bool_ else vec.astype(np.float32, copy=False)
+  mask = np.zeros(num_row, np.uint8)
+  mask[np.asarray(rows)] = 1
+  out = np.zeros(num_row, np.float64)
+  ab = np.zeros(num_row, np.float64)
+  lib().orc_jitconn_mv_rows(KINDS[kind], vec_kind, _p(vec), num_row, vec.shape[0], p0, p1, clen, seed,
+                            0 if variant == "gpu" else 1, _p(mask), _p(out), _p(ab))
+  return out[rows], ab[rows]
 
 
 # ---- CSR ---------------------------------------------------------------------

@@ -240,6 +240,18 @@ void orc_jitconn_mv(int32_t kind, int32_t vec_kind, const void* vec, int64_t num
   free(active);
 }
 
+/* orc_jitconn_mv with outdim_parallel = 1, restricted to the output rows flagged in row_mask:
+ * in the pull form every output row draws its connections from its own stream (seeded by the
+ * row), so a row's value does not depend on the others.  Unflagged rows are left at zero. */
+void orc_jitconn_mv_rows(int32_t kind, int32_t vec_kind, const void* vec, int64_t num_row, int64_t num_col,
+                         float p0, float p1, int32_t clen, uint32_t seed, int32_t variant,
+                         const uint8_t* row_mask, double* out64, double* abs64) {
+  memset(out64, 0, sizeof(double) * (size_t)num_row);
+  if (abs64) memset(abs64, 0, sizeof(double) * (size_t)num_row);
+  mv_ctx c = {vec_kind, 1, variant, kind, p0, vec, out64, abs64};
+  jitconn_walk(kind, p0, p1, clen, seed, num_row, num_col, 1, variant, row_mask, mv_visit, &c);
+}
+
 /* ------------------------------------------------------------------------ */
 /* event CSR and sparse CSR                                                  */
 /* ------------------------------------------------------------------------ */

@@ -47,6 +47,12 @@ void orc_jitconn_mv(int32_t kind, int32_t vec_kind, const void* vec, int64_t num
                     float p0, float p1, int32_t clen, uint32_t seed, int32_t outdim_parallel,
                     int32_t variant, double* out64, double* abs64);
 
+/* As orc_jitconn_mv with outdim_parallel = 1, computing only the rows flagged in row_mask
+ * (num_row bytes); the other rows of out64/abs64 are zero. */
+void orc_jitconn_mv_rows(int32_t kind, int32_t vec_kind, const void* vec, int64_t num_row, int64_t num_col,
+                         float p0, float p1, int32_t clen, uint32_t seed, int32_t variant,
+                         const uint8_t* row_mask, double* out64, double* abs64);
+
 /* ---- event CSR (brainpy/_src/math/event/_csr_matvec.py:321-412) ----
  * ev_kind: 0 = bool (uint8), 1 = float32 with `> 0` (Numba), 2 = float32 with `!= 0` (Taichi)
  * idx64: indices/indptr are int64 when 1, int32 when 0.

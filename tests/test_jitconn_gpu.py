@@ -134,3 +134,32 @@ def test_full_size_linearity(jc):
   # mean in-degree from active inputs ~ 0.02 * fan-in, reduced by the stripe quirk (no
   # column at step*k - 1 and none beyond 32*step - 1)
   assert 15.0 < float(y.double().mean()) < 21.0
+
+
+@pytest.mark.parametrize("odp", [True, False])
+def test_full_size_against_oracle(jc, orc, odp):
+  """4M x 4M just-in-time matrix, fan-in 1000, 2 % bool events, seed 42, element-wise against
+  the oracle's generation of the same streams.  Pull form (outdim_parallel): 300 sampled output
+  rows, each regenerated from its own stream.  Push form: every output row (the oracle walks
+  the active inputs' streams only).  Weight 1: exact integer counts, compared bit for bit;
+  weight 0.6: within 1e-5 scaled by the sum of the terms."""
+  from brainpy_gb300.connect import bernoulli_events
+  n = 4_000_000
+  p = 1000 / 4e6
+  clen = jc.conn_len(p)
+  ev = bernoulli_events(n, 0.02, seed=5)
+  ev_h = ev.cpu().numpy()
+  rng = np.random.default_rng(9)
+  rows = np.unique(np.concatenate([rng.integers(0, n, 296), [0, 1, n - 2, n - 1]]))
+  for w in (1.0, 0.6):
+    y = jc.event_mv_prob_homo(ev, w, p, 42, shape=(n, n), outdim_parallel=odp).cpu().numpy()
+    if odp:
+      y64, a64 = orc.jitconn_mv_rows("homo", ev_h, n, w, 0.0, clen, 42, rows)
+      y = y[rows]
+    else:
+      y64, a64 = orc.jitconn_mv("homo", ev_h, n, w, 0.0, clen, 42, False)
+    if w == 1.0:
+      np.testing.assert_array_equal(y, y64.astype(np.float32))
+      assert y64.sum() > 0
+    else:
+      assert scaled_err(y, y64, a64) < TOL

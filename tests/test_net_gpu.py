@@ -165,3 +165,55 @@ def test_spike_ring_reads_as_reference_delay(bplib):
       assert got == int(want[T]), (key, T, got, int(want[T]))
       sp = torch.tensor([((T + 1) >> j) & 1 for j in range(8)], dtype=torch.uint8, device="cuda")
       _lib.check(L.bp_spike_ring_record(_lib.ptr(sp), 8, _lib.ptr(ring), ring_len, T, None, st), "ring_record")
+
+
+def _jit_csr(orc, ne, ni, prob, seeds):
+  """The four just-in-time projections (E2E, E2I, I2E, I2I; shape (post, pre), pull form) as
+  explicit connections from the oracle's generation of the same streams, merged into the
+  oracle network's excitatory-row and inhibitory-row CSR matrices over all n post columns."""
+  from brainpy_gb300.math.jitconn import conn_len
+  clen = conn_len(prob)
+  pre_all, post_all = [], []
+  for s, (n_post, n_pre, post_off, pre_off) in zip(seeds, ((ne, ne, 0, 0), (ni, ne, ne, 0), (ne, ni, 0, ne),
+                                                           (ni, ni, ne, ne))):
+    rows, cols, _ = orc.jitconn_connections("homo", 1.0, 0.0, clen, s, n_post, n_pre, True, "gpu")
+    post_all.append(rows + post_off)
+    pre_all.append(cols + pre_off)
+  pre, post = np.concatenate(pre_all), np.concatenate(post_all)
+  order = np.argsort(pre, kind="stable")
+  pre, post = pre[order], post[order]
+  out = []
+  for lo, hi in ((0, ne), (ne, ne + ni)):
+    sel = (pre >= lo) & (pre < hi)
+    ptr = np.concatenate([[0], np.cumsum(np.bincount(pre[sel] - lo, minlength=hi - lo))]).astype(np.int32)
+    out += [ptr, np.ascontiguousarray(post[sel].astype(np.int32))]
+  return out
+
+
+def test_jitconn_network_against_oracle(dyn, orc):
+  """EINetwork(jitconn=...) -- the four EventJitFPHomoLinear projections (brainpy/_src/dnn/
+  linear.py:1044-1280) feeding the COBA outputs (align_post.py:271-275) -- run on the
+  per-operator path, host loop and CUDA-graph replay, against the oracle network on the same
+  connectivity regenerated by the oracle: spike counts of every step and the final state bit
+  for bit (homogeneous weights: exact event counts times w on both sides)."""
+  ne, ni, prob, seeds = 1600, 400, 0.05, (11, 12, 13, 14)
+  V0 = _v0(ne + ni, seed=21)
+  jit = dict(prob=prob, seeds=seeds)
+  a = dyn.EINetwork(ne + ni, ne, jitconn=jit, V0=V0)
+  b = dyn.EINetwork(ne + ni, ne, jitconn=jit, V0=V0)
+  state = a.state_numpy()
+  ca, _ = a.run(300, method="ops")
+  cb, _ = b.run(300, method="ops", graph_steps=50)
+  ep, ei, ip, ii = _jit_csr(orc, ne, ni, prob, seeds)
+  p = a.params
+  op = orc.lif_params(p.V_rest, p.V_th, p.V_reset, p.tau, p.tau_ref, p.R, p.tau_e, p.tau_i, p.E_e, p.E_i, p.input,
+                      p.ltc)
+  rc, _ = orc.coba_net_run(op, a.n, ne, ep, ei, np.float32(a.we), ip, ii, np.float32(a.wi), state, 0, 300,
+                           np.float32(0.1), count_mode=True)
+  np.testing.assert_array_equal(ca.cpu().numpy(), rc)
+  np.testing.assert_array_equal(cb.cpu().numpy(), rc)
+  for net in (a, b):
+    got = net.state_numpy()
+    for k in ("V", "ge", "gi", "t_last", "spike"):
+      np.testing.assert_array_equal(got[k], state[k], err_msg=k)
+  assert rc.sum() > 300  # the network is active

@@ -113,9 +113,15 @@ def test_planned_non_transpose_against_oracle(bplib, orc, tile_w):
   y = pw.sparse_n(xd).cpu().numpy()
   r = orc.csrmv(heter, ind_h, ptr_h, x, (m, n), False)
   assert scaled_err(y, r["out64"], r["abs64"]) < TOL
+  # the public call: rows of >= 256 entries on average go through the plan cache, shorter
+  # rows through the plain row kernel
   m2, n2 = 40000, 40000
-  ind2, ptr2 = fixed_prob_csr(m2, n2, 60, seed=2)
   x2 = torch.randn(n2, device="cuda")
-  y2 = sparse.csrmv(0.5, ind2, ptr2, x2, shape=(m2, n2), transpose=False).cpu().numpy()
-  r = orc.csrmv(np.float32(0.5), ind2.cpu().numpy(), ptr2.cpu().numpy(), x2.cpu().numpy(), (m2, n2), False)
-  assert scaled_err(y2, r["out64"], r["abs64"]) < TOL
+  for k2, planned in ((300, True), (60, False)):
+    ind2, ptr2 = fixed_prob_csr(m2, n2, k2, seed=2)
+    event.release_plans()
+    y2 = sparse.csrmv(0.5, ind2, ptr2, x2, shape=(m2, n2), transpose=False).cpu().numpy()
+    assert len(event._PLANS) == int(planned)
+    r = orc.csrmv(np.float32(0.5), ind2.cpu().numpy(), ptr2.cpu().numpy(), x2.cpu().numpy(), (m2, n2), False)
+    assert scaled_err(y2, r["out64"], r["abs64"]) < TOL
+  event.release_plans()

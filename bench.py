@@ -452,6 +452,8 @@ def north_star_forms(args):
       "plain_network_steps_per_s": r["plain_per_network_path"]["value"],
       "plain_sample": r["plain_per_network_path"]["sample"], "speedup_vs_plain": r["speedup_vs_plain"],
       "synaptic_events_per_s": r["synaptic_events_per_s"], "accuracy": r["accuracy"],
+      "untuned_network_steps_per_s": r["untuned_form"]["value"], "speedup_vs_untuned": r["speedup_vs_untuned"],
+      "tile_choices": r["tuning"]["choices"], "tuning_s": r["tuning"]["seconds"],
       "launches": r["gpu_launches"], "clocks": r["clocks"]}
   torch.cuda.empty_cache()
   from brainpy_gb300 import serve
@@ -556,7 +558,10 @@ def bench_coba(args):
 def bench_batched(args):
   """256 independent COBA networks, N ~ logU[1k, 64k], we ~ U[0.3, 1], wi ~ U[3, 10], 5000 steps,
   all in persistent cluster launches, against the plain per-network path (one network at a
-  time, one kernel per operator per step, host loop)."""
+  time, one kernel per operator per step, host loop).  The headline form runs autotuned tiles
+  (neurons per CTA chosen per size class, tuning outside the timed region) with the launches
+  of the different cluster sizes concurrent on side streams; the untuned form (default tiles,
+  launches in stream order) is timed from the same initial state beside it."""
   from brainpy_gb300 import dyn
   steps = args.sim_steps or 5000
   rng = np.random.default_rng(11)
@@ -572,10 +577,23 @@ def bench_batched(args):
   for x in nets:
     x._cluster_plan()
   k_plain = 20
+  # untuned form: the default tile rule, one launch per cluster size in stream order
+  counts0 = [torch.zeros(steps, dtype=torch.int32, device="cuda") for _ in nets]
+  launches0 = len({x.descriptor().n_tiles for x in nets})
+  t_untuned, _ = _cuda_time(lambda: dyn.run_networks(nets, steps, spike_counts=counts0, concurrent=False))
+  for x, st in zip(nets, init):
+    x.reset_state(*st)
+  from brainpy_gb300 import tuning
+  t0 = time.perf_counter()
+  tune = dyn.autotune_net_tiles(nets, cache=tuning.TuneCache())  # timed afresh (memory-only cache)
+  t_tune = time.perf_counter() - t0
+  for x in nets:
+    x._cluster_plan()
   counts = [torch.zeros(steps, dtype=torch.int32, device="cuda") for _ in nets]
   clocks = ClockSampler(torch.cuda.current_device())
   t_batch, _ = _cuda_time(lambda: dyn.run_networks(nets, steps, spike_counts=counts))
   clk = clocks.stop()
+  same_forms = all(torch.equal(a, b) for a, b in zip(counts0, counts))
   fan = np.array([int(0.8 * n * 0.02) + int((n - int(0.8 * n)) * 0.02) for n in sizes])
   n_spk = np.array([int(c.sum()) for c in counts])
   # plain path: every network from its initial state, k_plain steps each, one after another
@@ -604,7 +622,13 @@ def bench_batched(args):
           "plain_per_network_path": {"value": v_plain, "unit": "network-steps/s",
                                      "sample": f"all {len(nets)} networks x {k_plain} steps, per-operator kernels, host loop"},
           "speedup_vs_plain": v_batch / v_plain,
-          "accuracy": "bit-identical spike counts over the first %d steps of every network: %s" % (k_plain, same),
+          "untuned_form": {"value": len(nets) * steps / t_untuned, "unit": "network-steps/s",
+                           "form": "default tiles (a quarter of the network, >= 1024), launches in stream order",
+                           "launches": launches0},
+          "speedup_vs_untuned": t_untuned / t_batch,
+          "tuning": {"seconds": t_tune, "choices": {f"{k:+.1f}": v["choice"] for k, v in tune.items()}},
+          "accuracy": ("bit-identical spike counts over the first %d steps of every network: %s; "
+                       "tuned+concurrent equals untuned+ordered over all steps: %s") % (k_plain, same, same_forms),
           "clocks": clk, "gpu_launches": len({x.descriptor().n_tiles for x in nets})}
 
 

@@ -369,7 +369,9 @@ class EINetwork:
       buf = torch.zeros(graph_steps, dtype=torch.int32, device=self.device)
       g = torch.cuda.CUDAGraph()
       torch.cuda.synchronize()
-      with torch.cuda.graph(g):
+      # thread_local: another host thread (a server's job builder) may allocate while this
+      # thread captures; only this thread's calls are checked for capture safety
+      with torch.cuda.graph(g, capture_error_mode="thread_local"):
         for j in range(graph_steps):
           self.step_ops(dt, step_dev=step_dev, offset=j)
           buf[j] = self.spike.sum()
@@ -388,10 +390,24 @@ class EINetwork:
     return counts
 
 
-def run_networks(nets, steps, dt=0.1, spike_counts=None, v_traces=None, trace_steps=0, step_limits=None):
+_SIDE_STREAMS = {}  # device index -> side streams of run_networks
+
+
+def _side_streams(dev, k):
+  idx = dev.index if dev.index is not None else torch.cuda.current_device()
+  pool = _SIDE_STREAMS.setdefault(idx, [])
+  while len(pool) < k:
+    pool.append(torch.cuda.Stream(device=dev))
+  return pool[:k]
+
+
+def run_networks(nets, steps, dt=0.1, spike_counts=None, v_traces=None, trace_steps=0, step_limits=None,
+                 concurrent=True):
   """Runs every network for `steps` steps (or its own step limit) in persistent cluster
   launches, one launch per cluster size: networks of one size run concurrently, one cluster
-  each, each at its own time index."""
+  each, each at its own time index.  With `concurrent`, the launches go to side streams
+  forked from the current stream and joined back to it, so that a size class too small to
+  fill the GPU does not hold the others back; results do not depend on it."""
   if not nets:
     return
   dev = nets[0].device
@@ -403,12 +419,93 @@ def run_networks(nets, steps, dt=0.1, spike_counts=None, v_traces=None, trace_st
     groups.setdefault(d.n_tiles, []).append((net, d, lim))
   L = _lib.lib()
   keep = []
-  for cl, items in sorted(groups.items()):
+  # largest launches (CTAs) first: they set the run's length
+  launches = sorted(groups.items(), key=lambda kv: (-kv[0] * len(kv[1]), kv[0]))
+  for cl, items in launches:
     arr = (_lib.NetDesc * len(items))(*[d for _, d, _ in items])
-    buf = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(dev, non_blocking=False)
-    keep.append(buf)
-    st = L.bp_net_run(_lib.ptr(buf), len(items), cl, 0, int(steps), float(dt), _lib.stream_handle(dev))
+    keep.append(torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(dev, non_blocking=False))
+  cur = torch.cuda.current_stream(dev)
+  streams = _side_streams(dev, len(launches)) if concurrent and len(launches) > 1 else [cur]
+  for s in streams:
+    if s is not cur:
+      s.wait_stream(cur)
+  for (cl, items), buf, s in zip(launches, keep, streams * len(launches)):
+    with torch.cuda.stream(s):
+      st = L.bp_net_run(_lib.ptr(buf), len(items), cl, 0, int(steps), float(dt), _lib.stream_handle(dev))
     _lib.check(st, "net_run")
     for net, _, lim in items:
       net.t_step += min(steps, lim) if lim > 0 else steps
+  for s in streams:
+    if s is not cur:
+      cur.wait_stream(s)
   return keep
+
+
+def tile_candidates(n, candidates=(1024, 2048, 4096)):
+  """Neurons per CTA of the cluster runner that an n-neuron network can take: multiples of 64
+  within the runner's width, with at most the runner's maximum of CTAs per cluster."""
+  L = _lib.lib()
+  cap, tmax = L.bp_net_tile_width(), L.bp_net_max_tiles()
+  return [int(t) for t in candidates if t % 64 == 0 and 64 <= t <= cap and -(-int(n) // int(t)) <= tmax]
+
+
+def size_class(n):
+  """Half-octave size class of a network (round(2 log2 n) / 2): the unit of tile tuning."""
+  return round(2.0 * math.log2(max(int(n), 1))) / 2.0
+
+
+def autotune_net_tiles(nets, candidates=(1024, 2048, 4096), steps=100, cache=None):
+  """Chooses the cluster runner's neurons per CTA (and so the cluster shape, ceil(n / tile)
+  CTAs) for every network, per half-octave size class, and applies it (the networks' runner
+  plans are rebuilt on next use).
+
+  A class is timed on its median network: for each candidate tile, a copy of that network
+  (same connectivity, parameters and state) runs `steps` steps alone after a warm-up; the
+  choice minimises the device time a network-step takes from the GPU, the step time times
+  the CTAs it holds, which is what the throughput of a batch that fills the GPU depends on.
+  Choices are kept in the tuning cache (``tuning.default_cache()`` unless one is given) under
+  the device and class, so later batches and processes apply them without timing.  Results
+  do not depend on the tile.  Returns {class: record}."""
+  from . import tuning
+  cache = cache if cache is not None else tuning.default_cache()
+  classes = {}
+  for net in nets:
+    if net.jitconn is None:
+      classes.setdefault(size_class(net.n), []).append(net)
+  out = {}
+  for cls, members in sorted(classes.items()):
+    n_max = max(m.n for m in members)
+    cands = tile_candidates(n_max, candidates)
+    if not cands:
+      continue
+    dev = members[0].device
+    key = f"net_tile|{torch.cuda.get_device_name(dev)}|class={cls:+.1f}|cands={','.join(map(str, cands))}"
+    rec = cache.lookup(key)
+    if rec is None or int(rec.get("choice", -1)) not in cands:
+      rep = sorted(members, key=lambda m: m.n)[len(members) // 2]
+      cost, per_step = {}, {}
+      for t in cands:
+        probe = EINetwork(rep.n, rep.n_exc, indices=rep.indices, indptr=rep.indptr, we=rep.we, wi=rep.wi,
+                          params=rep.params, device=dev, V0=rep.V, net_tile=t)
+        probe.run(max(steps // 4, 1))  # plan build, module load, firing under way
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        probe.run(steps)
+        t1.record()
+        t1.synchronize()
+        us = t0.elapsed_time(t1) * 1e3 / steps
+        per_step[str(t)] = us
+        cost[str(t)] = us * (-(-rep.n // t))
+        del probe
+      best = min(cands, key=lambda t: (cost[str(t)], -t))
+      rec = {"choice": int(best), "cta_us_per_step": cost, "us_per_step": per_step, "timed_on_n": int(rep.n)}
+      cache.store(key, rec)
+      cache.save()
+    best = int(rec["choice"])
+    for m in members:
+      if m.net_tile != best:
+        m.net_tile = best
+        m._plan = None
+    out[cls] = rec
+  return out

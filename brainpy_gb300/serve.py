@@ -8,6 +8,10 @@ are regenerated from its LFSR88 streams).
 The loop:
   * admission: arrived jobs enter in FIFO order while their estimated device memory fits the
     HBM budget; state and connectivity then stay resident on the device until the job ends;
+  * building: an admitted job's network (FixedProb generation, plan, counters, workspaces) is
+    built on a worker thread into its own CUDA stream, so a burst of arrivals does not stall
+    the jobs already stepping; the job joins the stepping set once its build has finished on
+    the host, its streams ordered after the build by a CUDA event;
   * every iteration advances all admitted jobs by one chunk of steps: CSR jobs that fit one
     thread-block cluster (n <= 16 x 4096) run together in persistent cluster launches (one per
     cluster size, every network at its own time index and step limit); the others run their
@@ -19,7 +23,9 @@ A job's result does not depend on what it shares the device with: every path is 
 (integer event counts; homogeneous-weight atomics add equal values).
 """
 import math
+import threading
 import time
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass
 from typing import List, Optional
 
@@ -51,6 +57,7 @@ class Job:
   finished_at: float = -1.0
   result: Optional[np.ndarray] = None
   stream: Optional[torch.cuda.Stream] = None
+  built_by: str = ""  # the host thread that built the job
 
   @property
   def latency(self):
@@ -94,13 +101,16 @@ def build_job(job: Job, device) -> dyn.EINetwork:
 
 class Server:
   def __init__(self, hbm_budget_bytes: float = 150e9, chunk_steps: int = 100, dt: float = 0.1, side_streams: int = 4,
-               graph_steps: int = 50, device=None):
+               graph_steps: int = 50, device=None, build_thread: bool = True):
     self.budget = float(hbm_budget_bytes)
     self.chunk = int(chunk_steps)
     self.dt = float(dt)
     self.graph_steps = int(graph_steps)
     self.device = device or torch.device("cuda", torch.cuda.current_device())
     self.streams = [torch.cuda.Stream(device=self.device) for _ in range(side_streams)]
+    self.build_stream = torch.cuda.Stream(device=self.device) if self.device.type == "cuda" else None
+    self._pool = ThreadPoolExecutor(max_workers=1, thread_name_prefix="bp-serve-build") if build_thread else None
+    self.building = []  # (job, future of its build event), in admission order
     self.queue: List[Job] = []
     self.active: List[Job] = []
     self.done: List[Job] = []
@@ -122,18 +132,57 @@ class Server:
     while self.queue and self.queue[0].arrival <= t:
       job = self.queue[0]
       need = job_memory(job)
-      if self.used + need > self.budget and self.active:
+      if self.used + need > self.budget and (self.active or self.building):
         break  # wait for memory to free up (FIFO: no overtaking)
       self.queue.pop(0)
       job.mem = need
       self.used += need
       job.admitted_at = self.now()
+      if self._pool is not None:
+        self.building.append((job, self._pool.submit(self._build, job)))
+      else:
+        self._activate(job, self._build(job))
+    # jobs whose build has finished join the stepping set (a failed build raises here)
+    pending = []
+    for job, fut in self.building:
+      if fut.done():
+        self._activate(job, fut.result())
+      else:
+        pending.append((job, fut))
+    self.building = pending
+
+  def _build(self, job):
+    """The job's network, spike counters and the connectivity structures its path reads (the
+    cluster runner's plan, or the per-operator path's projection plans and workspaces), all
+    on the build stream.  Runs on the worker thread; returns a CUDA event recorded after the
+    last of that work."""
+    job.built_by = threading.current_thread().name
+    if self.build_stream is None:  # host-only use (no device work to order)
       job.net = build_job(job, self.device)
       job.counts = torch.zeros(job.steps_total, dtype=torch.int32, device=self.device)
-      if not self._fits_cluster(job):
-        job.stream = self.streams[job.jid % len(self.streams)]
-        job.stream.wait_stream(torch.cuda.current_stream(self.device))
-      self.active.append(job)
+      return None
+    torch.cuda.set_device(self.device)
+    with torch.cuda.stream(self.build_stream):
+      job.net = build_job(job, self.device)
+      job.counts = torch.zeros(job.steps_total, dtype=torch.int32, device=self.device)
+      if self._fits_cluster(job):
+        job.net._cluster_plan()
+      elif job.conn == "csr":
+        job.net._csr_ops()
+      ev = torch.cuda.Event()
+      ev.record(self.build_stream)
+    return ev
+
+  def _activate(self, job, built):
+    """Orders the job's stepping stream after its build and adds it to the stepping set."""
+    if built is None:
+      pass
+    elif self._fits_cluster(job):
+      torch.cuda.current_stream(self.device).wait_event(built)
+    else:
+      job.stream = self.streams[job.jid % len(self.streams)]
+      job.stream.wait_event(built)
+    self.active.append(job)
 
   def _fits_cluster(self, job):
     return job.conn == "csr" and job.n <= _lib.lib().bp_net_max_tiles() * _lib.lib().bp_net_tile_width()
@@ -178,16 +227,26 @@ class Server:
   def run(self, max_seconds: float = 1e9):
     """Serves every submitted job; returns wall seconds."""
     self.t0 = time.perf_counter()
-    while (self.queue or self.active) and self.now() < max_seconds:
+    while (self.queue or self.active or self.building) and self.now() < max_seconds:
       self._admit()
       if not self.active:
-        if self.queue:
+        if self.building:
+          time.sleep(0.0005)  # a build in flight: wait for it on the host
+        elif self.queue:
           time.sleep(max(0.0, min(0.01, self.queue[0].arrival - self.now())))
         continue
       self._advance()
       self._retire()
+    for _, fut in self.building:  # a time limit hit with builds in flight: let them finish
+      fut.result()
     torch.cuda.synchronize(self.device)
     return self.now()
+
+  def close(self):
+    """Stops the build thread."""
+    if self._pool is not None:
+      self._pool.shutdown(wait=True)
+      self._pool = None
 
 
 def poisson_jobs(n_jobs, rate_hz=50.0, n_min=4000, n_max=1_000_000, dur_ms=(100.0, 2000.0), seed=0,
@@ -213,6 +272,7 @@ def bench(args):
   for k, (n, conn) in enumerate([(5000, "csr"), (200_000, "csr"), (5000, "jitconn"), (200_000, "jitconn")]):
     warm.submit(Job(jid=k, n=n, conn=conn, duration_ms=20.0, we=0.6, wi=6.7, arrival=0.0, seed=7 + k))
   warm.run()
+  warm.close()
   del warm
   torch.cuda.synchronize()
   jobs = poisson_jobs(n_jobs)
@@ -220,6 +280,7 @@ def bench(args):
   for j in jobs:
     srv.submit(j)
   wall = srv.run()
+  srv.close()
   lat = np.array([j.latency for j in srv.done])
   steps = sum(j.steps_total for j in srv.done)
   # the plain per-network path on the same jobs: one job at a time, one kernel per operator per

@@ -217,3 +217,31 @@ def test_jitconn_network_against_oracle(dyn, orc):
     for k in ("V", "ge", "gi", "t_last", "spike"):
       np.testing.assert_array_equal(got[k], state[k], err_msg=k)
   assert rc.sum() > 300  # the network is active
+
+
+def test_autotuned_tiles_and_concurrent_launches_match(dyn):
+  """Networks of several size classes: tiles chosen by autotune_net_tiles and the launches of
+  the cluster sizes run concurrently give the same spike counts and state, bit for bit, as
+  the default tiles with the launches in stream order; a cached choice is applied without
+  timing."""
+  from brainpy_gb300 import tuning
+  sizes = [1500, 3000, 6000, 20000, 45000]
+  def make():
+    return [dyn.EINetwork.fixed_prob(int(0.8 * n), n - int(0.8 * n), seed=30 + k, V0=_v0(n, seed=40 + k))
+            for k, n in enumerate(sizes)]
+  a, b = make(), make()
+  ca = [torch.zeros(300, dtype=torch.int32, device="cuda") for _ in a]
+  cb = [torch.zeros(300, dtype=torch.int32, device="cuda") for _ in b]
+  dyn.run_networks(a, 300, spike_counts=ca, concurrent=False)
+  cache = tuning.TuneCache()
+  rec = dyn.autotune_net_tiles(b, steps=40, cache=cache)
+  assert rec and all(r["choice"] in (1024, 2048, 4096) for r in rec.values())
+  assert all(x.net_tile == rec[dyn.size_class(x.n)]["choice"] for x in b)
+  dyn.run_networks(b, 300, spike_counts=cb)
+  for x, y, c1, c2 in zip(a, b, ca, cb):
+    assert torch.equal(c1, c2) and torch.equal(x.V, y.V) and torch.equal(x.t_last, y.t_last)
+    assert int(c1.sum()) > 0
+  # the same classes again: the cached records are applied, nothing is timed
+  c = make()
+  rec2 = dyn.autotune_net_tiles(c, steps=40, cache=cache)
+  assert {k: v["choice"] for k, v in rec2.items()} == {k: v["choice"] for k, v in rec.items()}

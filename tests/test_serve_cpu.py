@@ -11,7 +11,7 @@ import brainpy_gb300.serve as serve
 
 def _server(monkeypatch, budget):
   monkeypatch.setattr(serve, "build_job", lambda job, device: object())
-  srv = serve.Server(hbm_budget_bytes=budget, side_streams=0, device=torch.device("cpu"))
+  srv = serve.Server(hbm_budget_bytes=budget, side_streams=0, device=torch.device("cpu"), build_thread=False)
   srv._fits_cluster = lambda job: True  # no side stream needed for a stubbed job
   return srv
 
@@ -104,3 +104,36 @@ def test_poisson_jobs_stream(n_jobs):
   assert all(j.conn in ("csr", "jitconn") for j in jobs)
   again = serve.poisson_jobs(n_jobs, seed=3)
   assert [(j.n, j.conn, j.arrival) for j in again] == [(j.n, j.conn, j.arrival) for j in jobs]
+
+
+def test_builds_run_off_the_scheduling_thread(monkeypatch):
+  """Admitted jobs are built by the worker thread; they join the stepping set on a later
+  admission pass once their build has finished, in admission order, and nothing is lost."""
+  import threading
+  gate = threading.Event()
+
+  def slow_build(job, device):
+    gate.wait(10.0)
+    return object()
+
+  monkeypatch.setattr(serve, "build_job", slow_build)
+  srv = serve.Server(hbm_budget_bytes=1e15, side_streams=0, device=torch.device("cpu"))
+  srv._fits_cluster = lambda job: True
+  try:
+    for j in _jobs([3000, 4000, 5000]):
+      srv.submit(j)
+    srv.t0 = 0.0
+    srv.now = lambda: 1.0
+    srv._admit()
+    # admitted (memory reserved) but still building: the scheduling thread did not wait
+    assert srv.active == [] and [j.jid for j, _ in srv.building] == [0, 1, 2]
+    assert srv.used == sum(serve.job_memory(j) for j, _ in srv.building)
+    gate.set()
+    for _, fut in list(srv.building):
+      fut.result(timeout=10.0)
+    srv._admit()
+    assert [j.jid for j in srv.active] == [0, 1, 2] and srv.building == []
+    assert all(j.built_by.startswith("bp-serve-build") for j in srv.active)
+  finally:
+    gate.set()
+    srv.close()

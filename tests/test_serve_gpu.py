@@ -51,6 +51,8 @@ def test_results_equal_alone(serve):
     ref = _alone(serve, j, dev)
     np.testing.assert_array_equal(j.result, ref, err_msg=f"job {j.jid} ({j.conn}, n={j.n})")
     assert j.result.sum() > 0 and j.latency > 0
+    assert j.built_by.startswith("bp-serve-build")  # built on the worker thread
+  srv.close()
 
 
 def test_budget_admission(serve):

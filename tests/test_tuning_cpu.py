@@ -115,3 +115,16 @@ def test_valid_choices(bplib):
   assert all(ev._valid_choice(f"tiled:{c}") for c in codes)
   for bad in ("tiled:999999", "tiled:x", "columns", None, 3):
     assert not ev._valid_choice(bad)
+
+
+def test_net_tile_candidates_and_classes(bplib):
+  from brainpy_gb300 import dyn
+  L = bplib
+  tmax, cap = L.bp_net_max_tiles(), L.bp_net_tile_width()
+  assert dyn.tile_candidates(1000) == [1024, 2048, 4096]
+  # a network may not need more CTAs than a cluster holds
+  n_big = tmax * 2048 + 1
+  assert dyn.tile_candidates(n_big) == [t for t in (4096,) if t <= cap]
+  assert dyn.tile_candidates(1000, (1000, 64, cap + 64)) == [64]
+  assert dyn.size_class(4000) == dyn.size_class(4200) != dyn.size_class(6000)
+  assert dyn.size_class(1) == 0.0

@@ -211,11 +211,13 @@ typedef struct {
 int32_t bp_csr_plan_default_tile(int64_t n, int32_t cluster);
 /* tile width of a counting plan for n columns, 0 when n is too small for one (n < 2^19).
  * A counting plan (bp_csr_plan.kind = 1) has tiles as wide as one CTA's shared memory holds
- * 32-bit counts (about 50K columns).  bp_event_csrmv_planned runs it with R CTAs per tile
- * (R = SMs / n_tiles, at most 16), each counting its share of the active rows, and a second
- * kernel that adds the R partial counts of every column (the workspace holds them).  A call
- * then reads fewer, longer segments than with the default tile: DRAM serves random reads of up
- * to ~128 bytes at a fixed rate, so the call is faster.  Counting plans serve homogeneous
+ * 16-bit counters packed in pairs (up to 65,472 columns).  bp_event_csrmv_planned runs it with
+ * R CTAs per tile (R = SMs / n_tiles, at most 16), each counting its share of the active rows,
+ * and a second kernel that adds the R partial counts of every column (the workspace holds
+ * them).  A call reads half as many, twice as long segments as with the default tile (DRAM
+ * serves random reads of up to ~128 bytes at a fixed rate), at the cost of the partial counts'
+ * round trip through the workspace; which is faster depends on the matrix and the rate, so
+ * it is a candidate for timing rather than a default.  Counting plans serve homogeneous
  * weights and single event vectors (BP_ENOTSUP for dense vectors and batches). */
 int32_t bp_csr_plan_count_tile(int64_t n);
 size_t bp_csr_plan_bytes(int64_t m, int64_t n, int64_t nnz, int32_t heter, int32_t tile_w);

@@ -550,8 +550,9 @@ constexpr int kSplitMaxTile = 65472;  // a multiple of 64; pads reach tile_w + 3
 // one half of the tile's columns), a multiple of 4
 __host__ __device__ inline int split_acc_words(int tile_w) { return ((tile_w + kPlanPadSpan) / 2 + 3) / 4 * 4; }
 static size_t split_table_bytes() { return sizeof(uint32_t) * (size_t)(2 * kFlatRows + kFlatRows / 32 + 2 * kFlatRounds); }
-static size_t split_smem_bytes(int tile_w) {
-  return sizeof(uint32_t) * (size_t)split_acc_words(tile_w) + sizeof(int) * (kBlockGroup + 1) + split_table_bytes();
+static size_t split_smem_bytes(int tile_w, bool tables = true) {
+  return sizeof(uint32_t) * (size_t)split_acc_words(tile_w) + sizeof(int) * (kBlockGroup + 1) +
+         (tables ? split_table_bytes() : 0);
 }
 
 struct SplitArgs {
@@ -566,6 +567,11 @@ struct SplitArgs {
   int32_t tile_w, n_tiles, nb, R;
 };
 
+// G == 0: the flat rounds above.  G > 0: warps walk slices of 32 active rows; groups of G lanes
+// take one segment each (lane gl loads chunks gl, gl + G, ..., RND in the first round, the
+// rest in a loop), and the loads of a slice's next round of segments are in flight while the
+// current round's adds issue.  No tables: fewer instructions a chunk than the flat rounds.
+template <int G, int RND>
 __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const SplitArgs a) {
   constexpr unsigned FULL = 0xffffffffu;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -667,6 +673,59 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const Sp
       else h = mid;
     }
     return __ldg(a.lists + (int64_t)(g0 + l) * kCompactRows + (j - s_boff[l]));
+  };
+
+  // slices of 32 active rows per warp, groups of G lanes per segment (G > 0)
+  auto run_groups = [&](int g0, int ng, int total) {
+    constexpr int GG = G > 0 ? G : 1;
+    constexpr int NG = 32 / GG;  // segments a round
+    const int grp = lane / GG, gl = lane % GG;
+    const int nslices = (total + 31) >> 5;
+    auto bounds = [&](int k, uint32_t& st, uint32_t& nch) {
+      const int i = (k << 5) + lane;
+      st = 0u;
+      nch = 0u;
+      if (k < nslices && i < total) {
+        const uint32_t* so = a.seg_off + (int64_t)row_of(g0, ng, i) * so_stride + tile;
+        st = __ldg(so);
+        nch = __ldg(so + 1) - st;
+      }
+    };
+    uint32_t st, nch, nst, nnch;
+    int k = warp;
+    bounds(k, st, nch);
+    for (; k < nslices; k += nwarps) {
+      bounds(k + nwarps, nst, nnch);  // the warp's next slice, in flight meanwhile
+      uint4 cur[RND], nxt[RND];
+      uint32_t cst, cn;
+      auto load = [&](uint4 (&v)[RND], int u, uint32_t& sst, uint32_t& sn) {
+        const int j = u * NG + grp;
+        sst = __shfl_sync(FULL, st, j);
+        sn = __shfl_sync(FULL, nch, j);
+#pragma unroll
+        for (int r = 0; r < RND; ++r) {
+          const uint32_t c = (uint32_t)(gl + r * GG);
+          v[r] = c < sn ? ld_stream_u4(a.idx + 8ull * (sst + c)) : pads;
+        }
+      };
+      load(cur, 0, cst, cn);
+#pragma unroll
+      for (int u = 0; u < GG; ++u) {
+        uint32_t xst = 0u, xn = 0u;
+        if (u + 1 < GG) load(nxt, u + 1, xst, xn);
+#pragma unroll
+        for (int r = 0; r < RND; ++r) add8(cur[r]);
+        for (uint32_t c = (uint32_t)(gl + RND * GG); c < cn; c += GG) add8(ld_stream_u4(a.idx + 8ull * (cst + c)));
+        if (u + 1 < GG) {
+#pragma unroll
+          for (int r = 0; r < RND; ++r) cur[r] = nxt[r];
+          cst = xst;
+          cn = xn;
+        }
+      }
+      st = nst;
+      nch = nnch;
+    }
   };
 
   // CTA-wide passes over the `total` active rows of one group: up to kFlatRows rows and
@@ -795,11 +854,14 @@ __global__ void __launch_bounds__(kTiledThreads, 1) ecsr_t_split_kernel(const Sp
   uint32_t* __restrict__ part = a.part + (size_t)blockIdx.x * (size_t)a.tile_w;
   auto run_all = [&]() {
     if (one_group) {
-      run_flat(b0, b1 - b0, rows);
+      if constexpr (G > 0) run_groups(b0, b1 - b0, rows);
+      else run_flat(b0, b1 - b0, rows);
     } else {
       for (int g0 = b0; g0 < b1; g0 += nthr) {
         const int ng = min(nthr, b1 - g0);
-        run_flat(g0, ng, group_prefix(g0, ng));
+        const int tot = group_prefix(g0, ng);
+        if constexpr (G > 0) run_groups(g0, ng, tot);
+        else run_flat(g0, ng, tot);
       }
     }
     __syncthreads();
@@ -1383,6 +1445,23 @@ static bp_status planned_batch(const char* who, const bp_csr_plan* plan, const f
 
 namespace bp {
 
+// Main-loop form of the split kernel: (G, RND) = (0, 1) for the flat rounds, otherwise G lanes
+// a segment and RND chunks a lane in the first round; BPGPU_SPLIT=G,RND overrides the default.
+// Measured at N = 1e6, K = 1000, 2 % (segments of ~62 entries): (4, 2) 31.5 us a call, (4, 3)
+// 31.5, (2, 4) 32.5, flat 32.9, (8, 1) 34.8, (8, 2) 35.3.
+static void split_variant(int& G, int& RND) {
+  G = 4;
+  RND = 2;
+  const char* e = getenv("BPGPU_SPLIT");
+  if (e) {
+    int g = 0, r = 0;
+    if (sscanf(e, "%d,%d", &g, &r) == 2) {
+      G = g;
+      RND = r;
+    }
+  }
+}
+
 static bp_status split_call(const bp_csr_plan* plan, const float* w_homo, const void* events, bp_etype etype,
                             float* out, void* workspace, cudaStream_t st) {
   PlanView v = plan_view(plan);
@@ -1406,19 +1485,28 @@ static bp_status split_call(const bp_csr_plan* plan, const float* w_homo, const 
   bp_status s = compact_blocked(events, etype, plan->m, 1, reinterpret_cast<int32_t*>(ws),
                                 reinterpret_cast<int32_t*>(ws + L.off_counts), st);
   if (s != BP_OK) return s;
-  static bool done[64] = {false};
-  BP_CUDA_TRY(prepare_kernel(ecsr_t_split_kernel, done));
+  int sg = 0, srnd = 1;
+  split_variant(sg, srnd);
+  void (*kfn)(const SplitArgs) = ecsr_t_split_kernel<0, 1>;
+  if (sg == 2 && srnd == 4) kfn = ecsr_t_split_kernel<2, 4>;
+  else if (sg == 4 && srnd == 2) kfn = ecsr_t_split_kernel<4, 2>;
+  else if (sg == 4 && srnd == 3) kfn = ecsr_t_split_kernel<4, 3>;
+  else if (sg == 8 && srnd == 1) kfn = ecsr_t_split_kernel<8, 1>;
+  else if (sg == 8 && srnd == 2) kfn = ecsr_t_split_kernel<8, 2>;
+  else sg = 0;
+  static bool done[8][64] = {};
+  BP_CUDA_TRY(prepare_kernel(kfn, done[(sg == 0 ? 0 : sg == 2 ? 1 : sg == 4 ? 2 + (srnd == 3) : 4 + (srnd == 2))]));
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(a.n_tiles * a.R), 1, 1);
   cfg.blockDim = dim3(kTiledThreads, 1, 1);
-  cfg.dynamicSmemBytes = split_smem_bytes(a.tile_w);
+  cfg.dynamicSmemBytes = split_smem_bytes(a.tile_w, sg == 0);
   cfg.stream = st;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  BP_CUDA_TRY(cudaLaunchKernelEx(&cfg, ecsr_t_split_kernel, a));
+  BP_CUDA_TRY(cudaLaunchKernelEx(&cfg, kfn, a));
   const int64_t groups = (int64_t)a.n_tiles * (a.tile_w >> 3);
   cudaLaunchConfig_t rcfg = {};
   rcfg.gridDim = dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>((groups + 255) / 256, (int64_t)device_sm_count() * 8)), 1, 1);

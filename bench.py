@@ -426,8 +426,9 @@ def main():
 
 
 def north_star_forms(args):
-  """The batched and served forms and the COBA example, each timed with CUDA events under its
-  own clock record, summarised beside the headline operator line."""
+  """The batched and served forms, the COBA example and the 4M-neuron jitconn network, each
+  timed with CUDA events under its own clock record, summarised beside the headline operator
+  line."""
   import copy
   out = {}
   a = copy.copy(args)
@@ -455,6 +456,15 @@ def north_star_forms(args):
       "untuned_network_steps_per_s": r["untuned_form"]["value"], "speedup_vs_untuned": r["speedup_vs_untuned"],
       "tile_choices": r["tuning"]["choices"], "tuning_s": r["tuning"]["seconds"],
       "launches": r["gpu_launches"], "clocks": r["clocks"]}
+  torch.cuda.empty_cache()
+  a = copy.copy(args)
+  a.sim_steps = 200
+  r = bench_jitconn_net(a)
+  out["jitconn_network"] = {
+      "config": r["config"]["workload"] + f", {r['steps']} steps timed", "steps_per_s": r["value"],
+      "ms_per_step": r["ms_per_step"], "connections_generated_per_s": r["connections_generated_per_s"],
+      "synaptic_events_per_s": r["synaptic_events_per_s"], "firing_rate_hz": r["firing_rate_hz"],
+      "clocks": r["clocks"]}
   torch.cuda.empty_cache()
   from brainpy_gb300 import serve
   a = copy.copy(args)

@@ -390,7 +390,95 @@ class EINetwork:
     return counts
 
 
-_SIDE_STREAMS = {}  # device index -> side streams of run_networks
+class NetBatch:
+  """A fixed set of networks simulated together by the persistent cluster runner: one launch
+  per cluster size (networks of one size run concurrently, one cluster each, each at its own
+  time index and step limit), the launches of the different sizes concurrent on side streams
+  forked from the current stream and joined back to it.
+
+  The descriptors live in device buffers that are rewritten (from pinned host memory, on the
+  current stream) before every run, so the launches can be captured once as a CUDA graph
+  (``capture``) and the whole batch then advances by one graph launch per ``replay``: every
+  replay continues each network from its current time index, with new spike-count outputs
+  and step limits.  Results do not depend on the form."""
+
+  def __init__(self, nets, dt=0.1, concurrent=True):
+    self.nets = list(nets)
+    self.dt = float(dt)
+    self.dev = self.nets[0].device if self.nets else None
+    groups = {}
+    for k, net in enumerate(self.nets):
+      groups.setdefault(net.descriptor().n_tiles, []).append(k)
+    # largest launches (CTAs) first: they set the run's length
+    self.groups = sorted(groups.items(), key=lambda kv: (-kv[0] * len(kv[1]), kv[0]))
+    sz = ctypes.sizeof(_lib.NetDesc)
+    self._desc = [torch.empty(len(ix) * sz, dtype=torch.uint8, device=self.dev) for _, ix in self.groups]
+    self.concurrent = bool(concurrent)
+    self._graph = None
+
+  @property
+  def launches(self):
+    return len(self.groups)
+
+  def _write(self, spike_counts, step_limits, v_traces, trace_steps):
+    for (_, ix), dbuf in zip(self.groups, self._desc):
+      arr = (_lib.NetDesc * len(ix))(*[
+          self.nets[k].descriptor(spike_counts[k] if spike_counts else None, None,
+                                  v_traces[k] if v_traces else None, trace_steps,
+                                  int(step_limits[k]) if step_limits is not None else 0) for k in ix])
+      host = torch.empty(dbuf.numel(), dtype=torch.uint8, pin_memory=True)
+      ctypes.memmove(host.data_ptr(), ctypes.addressof(arr), ctypes.sizeof(arr))
+      dbuf.copy_(host, non_blocking=True)  # the pinned block is reused only after the copy
+
+  def _launches(self, steps):
+    L = _lib.lib()
+    cur = torch.cuda.current_stream(self.dev)
+    streams = _side_streams(self.dev, len(self.groups)) if self.concurrent and len(self.groups) > 1 else [cur]
+    for s in streams:
+      if s is not cur:
+        s.wait_stream(cur)
+    for (cl, ix), dbuf, s in zip(self.groups, self._desc, streams * len(self.groups)):
+      with torch.cuda.stream(s):
+        st = L.bp_net_run(_lib.ptr(dbuf), len(ix), cl, 0, int(steps), self.dt, _lib.stream_handle(self.dev))
+      _lib.check(st, "net_run")
+    for s in streams:
+      if s is not cur:
+        cur.wait_stream(s)
+
+  def _advance(self, steps, step_limits):
+    for k, net in enumerate(self.nets):
+      lim = int(step_limits[k]) if step_limits is not None else 0
+      net.t_step += min(steps, lim) if lim > 0 else steps
+
+  def run(self, steps, spike_counts=None, step_limits=None, v_traces=None, trace_steps=0):
+    """Advances every network by `steps` steps (or its step limit)."""
+    if not self.nets or steps <= 0:
+      return
+    self._write(spike_counts, step_limits, v_traces, trace_steps)
+    self._launches(steps)
+    self._advance(steps, step_limits)
+
+  def capture(self, steps):
+    """Captures the launches of a `steps`-step run as one CUDA graph (nothing runs)."""
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize(self.dev)
+    with torch.cuda.graph(g, capture_error_mode="thread_local"):
+      self._launches(steps)
+    self._graph = (int(steps), g)
+    return g
+
+  def replay(self, spike_counts=None, step_limits=None):
+    """One launch of the captured graph: every network advances by the captured number of
+    steps (or its step limit), from its current time index."""
+    if self._graph is None:
+      raise RuntimeError("capture() the batch first")
+    steps, g = self._graph
+    self._write(spike_counts, step_limits, None, 0)
+    g.replay()
+    self._advance(steps, step_limits)
+
+
+_SIDE_STREAMS = {}  # device index -> side streams of the batched runner
 
 
 def _side_streams(dev, k):
@@ -404,41 +492,15 @@ def _side_streams(dev, k):
 def run_networks(nets, steps, dt=0.1, spike_counts=None, v_traces=None, trace_steps=0, step_limits=None,
                  concurrent=True):
   """Runs every network for `steps` steps (or its own step limit) in persistent cluster
-  launches, one launch per cluster size: networks of one size run concurrently, one cluster
-  each, each at its own time index.  With `concurrent`, the launches go to side streams
-  forked from the current stream and joined back to it, so that a size class too small to
-  fill the GPU does not hold the others back; results do not depend on it."""
+  launches (a one-off NetBatch): one launch per cluster size, networks of one size
+  concurrently, one cluster each, each at its own time index.  With `concurrent`, the
+  launches of the different sizes run concurrently on side streams; results do not depend
+  on it.  Returns the batch (its descriptor buffers stay valid while it is held)."""
   if not nets:
-    return
-  dev = nets[0].device
-  groups = {}
-  for k, net in enumerate(nets):
-    lim = int(step_limits[k]) if step_limits is not None else 0
-    d = net.descriptor(spike_counts[k] if spike_counts else None, None,
-                       v_traces[k] if v_traces else None, trace_steps, lim)
-    groups.setdefault(d.n_tiles, []).append((net, d, lim))
-  L = _lib.lib()
-  keep = []
-  # largest launches (CTAs) first: they set the run's length
-  launches = sorted(groups.items(), key=lambda kv: (-kv[0] * len(kv[1]), kv[0]))
-  for cl, items in launches:
-    arr = (_lib.NetDesc * len(items))(*[d for _, d, _ in items])
-    keep.append(torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8).to(dev, non_blocking=False))
-  cur = torch.cuda.current_stream(dev)
-  streams = _side_streams(dev, len(launches)) if concurrent and len(launches) > 1 else [cur]
-  for s in streams:
-    if s is not cur:
-      s.wait_stream(cur)
-  for (cl, items), buf, s in zip(launches, keep, streams * len(launches)):
-    with torch.cuda.stream(s):
-      st = L.bp_net_run(_lib.ptr(buf), len(items), cl, 0, int(steps), float(dt), _lib.stream_handle(dev))
-    _lib.check(st, "net_run")
-    for net, _, lim in items:
-      net.t_step += min(steps, lim) if lim > 0 else steps
-  for s in streams:
-    if s is not cur:
-      cur.wait_stream(s)
-  return keep
+    return None
+  b = NetBatch(nets, dt, concurrent=concurrent)
+  b.run(steps, spike_counts=spike_counts, step_limits=step_limits, v_traces=v_traces, trace_steps=trace_steps)
+  return b
 
 
 def tile_candidates(n, candidates=(1024, 2048, 4096)):

@@ -245,3 +245,28 @@ def test_autotuned_tiles_and_concurrent_launches_match(dyn):
   c = make()
   rec2 = dyn.autotune_net_tiles(c, steps=40, cache=cache)
   assert {k: v["choice"] for k, v in rec2.items()} == {k: v["choice"] for k, v in rec.items()}
+
+
+def test_batch_graph_replays_continue(dyn):
+  """NetBatch: the launches captured once as a CUDA graph and replayed twice (new spike-count
+  outputs and a step limit on the second replay) give what two plain batched runs give."""
+  sizes = [2000, 5000, 12000]
+  def make():
+    return [dyn.EINetwork.fixed_prob(int(0.8 * n), n - int(0.8 * n), seed=50 + k, V0=_v0(n, seed=60 + k))
+            for k, n in enumerate(sizes)]
+  a, b = make(), make()
+  lim = [0, 90, 0]
+  ca = [[torch.zeros(120, dtype=torch.int32, device="cuda") for _ in a] for _ in range(2)]
+  cb = [[torch.zeros(120, dtype=torch.int32, device="cuda") for _ in b] for _ in range(2)]
+  dyn.run_networks(a, 120, spike_counts=ca[0])
+  dyn.run_networks(a, 120, spike_counts=ca[1], step_limits=lim)
+  batch = dyn.NetBatch(b)
+  batch.capture(120)
+  batch.replay(spike_counts=cb[0])
+  batch.replay(spike_counts=cb[1], step_limits=lim)
+  for r in range(2):
+    for x, y in zip(ca[r], cb[r]):
+      assert torch.equal(x, y)
+  for x, y in zip(a, b):
+    assert x.t_step == y.t_step and torch.equal(x.V, y.V) and torch.equal(x.spike, y.spike)
+  assert [x.t_step for x in b] == [240, 210, 240]

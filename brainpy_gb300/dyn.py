@@ -179,8 +179,8 @@ class EINetwork:
         raise ValueError(f"network of {self.n} neurons exceeds one cluster ({_lib.lib().bp_net_max_tiles()} tiles)")
     return self._plan
 
-  def descriptor(self, spike_counts=None, raster=None, v_trace=None, trace_steps=0, step_limit=0):
-    plan = self._cluster_plan()
+  def descriptor(self, spike_counts=None, raster=None, v_trace=None, trace_steps=0, step_limit=0, plan=None):
+    plan = plan if plan is not None else self._cluster_plan()
     so, idx, w = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
     _lib.check(_lib.lib().bp_csr_plan_arrays(ctypes.byref(plan.c), ctypes.byref(so), ctypes.byref(idx),
                                              ctypes.byref(w)), "csr_plan_arrays")
@@ -201,6 +201,57 @@ class EINetwork:
     d.delay_e, d.delay_i, d.ring_len = self.d_e, self.d_i, self.ring_len
     d.ring = self.ring.data_ptr() if self.ring is not None else None
     return d
+
+  def fits_cluster(self):
+    """Whether the cluster runner (one thread-block cluster per network) can hold the network."""
+    L = _lib.lib()
+    return self.jitconn is None and self.n <= L.bp_net_max_tiles() * L.bp_net_tile_width()
+
+  # ---- whole-GPU persistent form (networks larger than a cluster) ----------------------
+  def grid_eligible(self):
+    """Whether the network can run in one persistent launch over the GPU (bp_net_run_grid):
+    CSR connectivity, no synaptic delay, every tile's cluster resident at once, and no column
+    with 65,536 or more incoming entries (the runner counts excitatory and inhibitory events
+    in the two 16-bit halves of one word)."""
+    if self.jitconn is not None or self.ring is not None:
+      return False
+    if _lib.lib().bp_net_grid_tile(self.n) <= 0:
+      return False
+    if not hasattr(self, "_indeg_ok"):
+      deg = torch.bincount(self.indices.to(torch.int64), minlength=self.n)
+      self._indeg_ok = bool(int(deg.max()) < 65536) if deg.numel() else True
+    return self._indeg_ok
+
+  def _grid_state(self):
+    """The runner's plan (tiles of bp_net_grid_tile(n) columns) and workspace, built once."""
+    if getattr(self, "_grid", None) is None:
+      if not self.grid_eligible():
+        raise ValueError(f"network of {self.n} neurons cannot run on the grid runner (jitconn, delays, too many "
+                         "tiles for the resident clusters, or a column with 65,536 or more inputs)")
+      L = _lib.lib()
+      tw = int(L.bp_net_grid_tile(self.n))
+      plan = _event.CSRPlan(self.indices, self.indptr, (self.n, self.n), tile_w=tw, cluster=1)
+      ws = _lib.workspace(L.bp_net_grid_workspace_size(self.n, tw), self.device)
+      self._grid = (plan, ws)
+    return self._grid
+
+  def _run_grid(self, steps, dt, counts, trace, trace_steps):
+    plan, ws = self._grid_state()
+    d = self.descriptor(counts, None, trace, trace_steps, 0, plan=plan)
+    st = _lib.lib().bp_net_run_grid(ctypes.byref(d), 0, int(steps), float(dt), _lib.ptr(ws), ws.numel(),
+                                    _lib.stream_handle(self.device))
+    _lib.check(st, "net_run_grid")
+    self.t_step += steps
+
+  def grid_error(self):
+    """The grid runner's error word after its last run (0: every barrier wait ended); waits
+    for the run."""
+    if getattr(self, "_grid", None) is None:
+      return 0
+    err = ctypes.c_int32(0)
+    _lib.check(_lib.lib().bp_net_grid_error(_lib.ptr(self._grid[1]), ctypes.byref(err),
+                                            _lib.stream_handle(self.device)), "net_grid_error")
+    return int(err.value)
 
   # ---- per-operator form ------------------------------------------------------------
   def _csr_split(self):
@@ -326,11 +377,19 @@ class EINetwork:
 
   def run(self, steps, dt=0.1, method="cluster", spike_counts=None, v_trace_steps=0, graph_steps=0):
     """Advances `steps` steps.  Returns (spike counts per step [steps] int32, V trace or None).
-    method "cluster": one persistent launch; "ops": per-operator launches, replayed from a
-    CUDA graph of `graph_steps` steps when graph_steps > 0."""
+    method "cluster": one persistent launch, on one thread-block cluster when the network
+    fits one (n <= 16 x 4096), otherwise over the whole GPU (bp_net_run_grid; see
+    ``grid_eligible``); "grid": the whole-GPU runner; "ops": per-operator launches, replayed
+    from a CUDA graph of `graph_steps` steps when graph_steps > 0."""
     counts = spike_counts if spike_counts is not None else torch.zeros(steps, dtype=torch.int32, device=self.device)
     if self.ring is not None and abs(float(dt) - self.delay_dt) > 1e-12:
       raise ValueError(f"the delays were counted in steps of dt={self.delay_dt}; run with that dt, not {dt}")
+    if method == "cluster" and not self.fits_cluster():
+      method = "grid"
+    if method == "grid":
+      trace = torch.empty((v_trace_steps, self.n), device=self.device) if v_trace_steps else None
+      self._run_grid(steps, dt, counts, trace, v_trace_steps)
+      return counts, trace
     if method == "cluster":
       trace = torch.empty((v_trace_steps, self.n), device=self.device) if v_trace_steps else None
       run_networks([self], steps, dt, spike_counts=[counts], v_traces=[trace] if trace is not None else None,

@@ -14,7 +14,8 @@ The loop:
     the host, its streams ordered after the build by a CUDA event;
   * every iteration advances all admitted jobs by one chunk of steps: CSR jobs that fit one
     thread-block cluster (n <= 16 x 4096) run together in persistent cluster launches (one per
-    cluster size, every network at its own time index and step limit); the others run their
+    cluster size, every network at its own time index and step limit); larger CSR jobs run
+    one whole-GPU persistent launch each (bp_net_run_grid); the jitconn jobs run their
     per-operator steps from per-job CUDA graphs spread over side streams, so their kernels
     overlap on the device;
   * finished jobs are retired (spike counts copied to the host, memory released) and their
@@ -58,6 +59,7 @@ class Job:
   result: Optional[np.ndarray] = None
   stream: Optional[torch.cuda.Stream] = None
   built_by: str = ""  # the host thread that built the job
+  path: str = ""      # "cluster", "grid" or "ops": how the job steps
 
   @property
   def latency(self):
@@ -160,15 +162,22 @@ class Server:
     if self.build_stream is None:  # host-only use (no device work to order)
       job.net = build_job(job, self.device)
       job.counts = torch.zeros(job.steps_total, dtype=torch.int32, device=self.device)
+      job.path = "cluster" if self._fits_cluster(job) else "ops"
       return None
     torch.cuda.set_device(self.device)
     with torch.cuda.stream(self.build_stream):
       job.net = build_job(job, self.device)
       job.counts = torch.zeros(job.steps_total, dtype=torch.int32, device=self.device)
       if self._fits_cluster(job):
+        job.path = "cluster"
         job.net._cluster_plan()
-      elif job.conn == "csr":
-        job.net._csr_ops()
+      elif job.conn == "csr" and job.net.grid_eligible():
+        job.path = "grid"
+        job.net._grid_state()
+      else:
+        job.path = "ops"
+        if job.conn == "csr":
+          job.net._csr_ops()
       ev = torch.cuda.Event()
       ev.record(self.build_stream)
     return ev
@@ -177,7 +186,7 @@ class Server:
     """Orders the job's stepping stream after its build and adds it to the stepping set."""
     if built is None:
       pass
-    elif self._fits_cluster(job):
+    elif job.path in ("cluster", "grid"):
       torch.cuda.current_stream(self.device).wait_event(built)
     else:
       job.stream = self.streams[job.jid % len(self.streams)]
@@ -188,7 +197,7 @@ class Server:
     return job.conn == "csr" and job.n <= _lib.lib().bp_net_max_tiles() * _lib.lib().bp_net_tile_width()
 
   def _advance(self):
-    cl = [j for j in self.active if self._fits_cluster(j)]
+    cl = [j for j in self.active if j.path == "cluster"]
     if cl:
       limits = [min(self.chunk, j.steps_total - j.steps_done) for j in cl]
       outs = [j.counts[j.steps_done:] for j in cl]
@@ -196,7 +205,15 @@ class Server:
       for j, k in zip(cl, limits):
         j.steps_done += k
     for j in self.active:
-      if self._fits_cluster(j):
+      if j.path != "grid":
+        continue
+      # one whole-GPU persistent launch per job and chunk, in turn on the current stream (each
+      # holds a cluster on every SM it uses while it runs)
+      k = min(self.chunk, j.steps_total - j.steps_done)
+      j.net.run(k, self.dt, method="grid", spike_counts=j.counts[j.steps_done:j.steps_done + k])
+      j.steps_done += k
+    for j in self.active:
+      if j.path != "ops":
         continue
       k = min(self.chunk, j.steps_total - j.steps_done)
       with torch.cuda.stream(j.stream):

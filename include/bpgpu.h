@@ -376,6 +376,31 @@ bp_status bp_net_run(const bp_net_desc* descs_device, int32_t num_nets, int32_t 
                      int32_t steps, float dt, bp_stream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * One E/I COBA network larger than a cluster, in one persistent launch over the GPU (the
+ * DSRunner loop of examples/dynamics_simulation/COBA.py run by brainpy/_src/runners.py:619-665;
+ * no reference counterpart as a kernel).  The network's plan (bp_csr_plan of the merged CSR
+ * over all n rows and columns) has tiles of tile_w = bp_net_grid_tile(n) columns; each tile is
+ * owned by a cluster of 4 CTAs, every CTA updating a quarter of the tile's neurons.  Each step
+ * propagates the previous step's spikes (exact integer counts, excitatory and inhibitory rows
+ * counted separately; no column may have 65,536 or more incoming entries), updates the neurons
+ * (dg = count * w, the LIF step of bp_lif_coba_step) and lists the new spikes, then waits on a
+ * grid-wide barrier whose waits are bounded: a wait that runs out ends the launch early and
+ * sets the error word that bp_net_grid_error reads.  Synaptic delays and rasters are not
+ * supported here (BP_ENOTSUP); desc is a host pointer.
+ * ------------------------------------------------------------------------- */
+/* tile width for an n-neuron network, 0 when its clusters cannot all be resident at once */
+int32_t bp_net_grid_tile(int64_t n);
+size_t bp_net_grid_workspace_size(int64_t n, int32_t tile_w);
+bp_status bp_net_run_grid(const bp_net_desc* desc, int32_t step0, int32_t steps, float dt, void* workspace,
+                          size_t workspace_bytes, bp_stream_t stream);
+/* the error word of the last run on this workspace (0: every barrier wait ended); synchronises */
+bp_status bp_net_grid_error(const void* workspace, int32_t* error, bp_stream_t stream);
+/* 1 when the last bp_net_run_grid launched with cooperative scheduling, 0 when the device refused
+ * cooperative scheduling together with clusters and the launch went without it (every cluster
+ * was checked to be resident at once), -1 before the first launch */
+int32_t bp_net_grid_cooperative(void);
+
+/* ---------------------------------------------------------------------------
  * Kernel timing (benchmark support; no reference counterpart).
  * When enabled, each operator's dominant kernel launch is bracketed by CUDA events on its
  * stream; bp_timer_collect synchronises them and returns the summed time and launch count,

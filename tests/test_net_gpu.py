@@ -270,3 +270,44 @@ def test_batch_graph_replays_continue(dyn):
   for x, y in zip(a, b):
     assert x.t_step == y.t_step and torch.equal(x.V, y.V) and torch.equal(x.spike, y.spike)
   assert [x.t_step for x in b] == [240, 210, 240]
+
+
+def _big_net(dyn, n, prob, seed, V0seed):
+  ne = int(0.8 * n)
+  s = 80.0 / (prob * n)  # COBA's total drive at this fan-out
+  return dyn.EINetwork.fixed_prob(ne, n - ne, prob=prob, we=0.6 * s, wi=6.7 * s, seed=seed, V0=_v0(n, seed=V0seed))
+
+
+def test_grid_runner_against_oracle(dyn, orc):
+  """A network larger than one cluster (100,000 neurons, fan-out 1000) in one persistent launch
+  over the GPU: spike counts of every step, the V trace of the first 50 steps and the final
+  state bit-exact against the oracle network; the barrier waits all ended."""
+  net = _big_net(dyn, 100_000, 0.01, seed=7, V0seed=8)
+  assert not net.fits_cluster() and net.grid_eligible()
+  state = net.state_numpy()
+  counts, trace = net.run(300, v_trace_steps=50)  # method "cluster" takes the grid runner here
+  assert net.grid_error() == 0
+  from brainpy_gb300 import _lib
+  print("grid runner cooperative launch:", _lib.lib().bp_net_grid_cooperative())
+  rc, rtrace = _oracle_run(orc, net, state, 300, trace_steps=50)
+  np.testing.assert_array_equal(counts.cpu().numpy(), rc)
+  np.testing.assert_array_equal(trace.cpu().numpy(), rtrace)
+  got = net.state_numpy()
+  for k in ("V", "ge", "gi", "t_last", "spike"):
+    np.testing.assert_array_equal(got[k], state[k], err_msg=k)
+  assert rc.sum() > 10_000
+
+
+def test_grid_runner_matches_ops_path_across_calls(dyn):
+  """300,000 neurons: two grid runs of 100 steps equal one per-operator run of 200 steps (graph
+  replay), bit for bit."""
+  a = _big_net(dyn, 300_000, 0.001, seed=9, V0seed=10)
+  b = dyn.EINetwork(a.n, a.n_exc, indices=a.indices, indptr=a.indptr, we=a.we, wi=a.wi, V0=a.V.clone())
+  c1, _ = a.run(100, method="grid")
+  c2, _ = a.run(100, method="grid")
+  cb, _ = b.run(200, method="ops", graph_steps=50)
+  assert a.grid_error() == 0
+  assert torch.equal(torch.cat([c1, c2]), cb)
+  for k in ("V", "ge", "gi", "t_last", "spike"):
+    assert torch.equal(getattr(a, k), getattr(b, k)), k
+  assert int(cb.sum()) > 1000 and a.t_step == 200

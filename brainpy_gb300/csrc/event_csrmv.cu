@@ -9,9 +9,13 @@
 // Reference semantics: brainpy/_src/math/event/_csr_matvec.py:321-412 (Numba CPU),
 // brainpy/_src/math/event/_csr_matvec_taichi.py:158-312 (Taichi GPU: warp per row,
 // global atomics).
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "compact.cuh"
 #include "timer.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace bp {
 
@@ -196,28 +200,24 @@ constexpr int64_t kSmallMaxNnz = 1 << 19;       // worst case (every row active)
 
 static size_t small_smem_bytes(int64_t n) { return sizeof(uint32_t) * ((size_t)n + kSmallRound + 1); }
 
+// Rows [r_begin, r_end) of a transposed product into the shared-memory accumulator `acc`
+// (n words: u32 counts, or f32 sums): rounds of kSmallRound events compacted into the shared
+// row list `rows`, then one warp per listed row, up to 128 entries a load round.
 template <typename IdxT, bool HOMO, int ET>
-__global__ void __launch_bounds__(kSmallThreads) ecsr_t_small_kernel(const IdxT* __restrict__ indptr,
-                                                                     const IdxT* __restrict__ indices,
-                                                                     const float* __restrict__ data, int64_t nnz,
-                                                                     int64_t m, int64_t n,
-                                                                     const void* __restrict__ events,
-                                                                     float* __restrict__ out) {
-  extern __shared__ uint32_t sm_small[];
-  uint32_t* acc = sm_small;                          // n words
-  int32_t* rows = reinterpret_cast<int32_t*>(sm_small + n);  // kSmallRound row ids
-  int32_t* n_rows = rows + kSmallRound;
+__device__ __forceinline__ void small_scatter(uint32_t* acc, int32_t* rows, int32_t* n_rows, int64_t r_begin,
+                                              int64_t r_end, const IdxT* __restrict__ indptr,
+                                              const IdxT* __restrict__ indices, const float* __restrict__ data,
+                                              int64_t nnz, int64_t n, const void* __restrict__ events) {
   const int lane = lane_id(), warp = threadIdx.x >> 5;
   constexpr int kWarps = kSmallThreads / 32;
-  for (int64_t i = threadIdx.x; i < n; i += kSmallThreads) acc[i] = 0u;
-  for (int64_t r0 = 0; r0 < m; r0 += kSmallRound) {
+  for (int64_t r0 = r_begin; r0 < r_end; r0 += kSmallRound) {
     if (threadIdx.x == 0) *n_rows = 0;
     __syncthreads();  // accumulators zeroed / previous round's list consumed
     bool on[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int64_t r = r0 + u * kSmallThreads + threadIdx.x;
-      on[u] = r < m && event_at<ET>(events, r);
+      on[u] = r < r_end && event_at<ET>(events, r);
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
@@ -253,13 +253,66 @@ __global__ void __launch_bounds__(kSmallThreads) ecsr_t_small_kernel(const IdxT*
     }
     __syncthreads();  // the list is reused by the next round
   }
-  if (m <= 0) __syncthreads();
+}
+
+template <typename IdxT, bool HOMO, int ET>
+__global__ void __launch_bounds__(kSmallThreads) ecsr_t_small_kernel(const IdxT* __restrict__ indptr,
+                                                                     const IdxT* __restrict__ indices,
+                                                                     const float* __restrict__ data, int64_t nnz,
+                                                                     int64_t m, int64_t n,
+                                                                     const void* __restrict__ events,
+                                                                     float* __restrict__ out) {
+  extern __shared__ uint32_t sm_small[];
+  uint32_t* acc = sm_small;                                  // n words
+  int32_t* rows = reinterpret_cast<int32_t*>(sm_small + n);  // kSmallRound row ids
+  int32_t* n_rows = rows + kSmallRound;
+  for (int64_t i = threadIdx.x; i < n; i += kSmallThreads) acc[i] = 0u;
+  small_scatter<IdxT, HOMO, ET>(acc, rows, n_rows, 0, m, indptr, indices, data, nnz, n, events);
+  __syncthreads();
   if (HOMO) {
     const float w0 = data[0];
     for (int64_t i = threadIdx.x; i < n; i += kSmallThreads) out[i] = (float)acc[i] * w0;
   } else {
     for (int64_t i = threadIdx.x; i < n; i += kSmallThreads) out[i] = __uint_as_float(acc[i]);
   }
+}
+
+// The same with one thread-block cluster of C CTAs, for small outputs with more work than one
+// SM does quickly: every CTA holds all n columns, takes 1/C of the rows (scanning their events
+// itself), and after a cluster barrier sums column slice q of the C accumulators through
+// distributed shared memory (in rank order) and writes it.  Still one launch, no global
+// atomics, no memset.
+template <typename IdxT, bool HOMO, int ET>
+__global__ void __launch_bounds__(kSmallThreads, 1) ecsr_t_cluster_small_kernel(const IdxT* __restrict__ indptr,
+                                                                                const IdxT* __restrict__ indices,
+                                                                                const float* __restrict__ data,
+                                                                                int64_t nnz, int64_t m, int64_t n,
+                                                                                const void* __restrict__ events,
+                                                                                float* __restrict__ out) {
+  extern __shared__ uint32_t sm_small[];
+  uint32_t* acc = sm_small;
+  int32_t* rows = reinterpret_cast<int32_t*>(sm_small + n);
+  int32_t* n_rows = rows + kSmallRound;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = (int)cluster.num_blocks(), q = (int)cluster.block_rank();
+  for (int64_t i = threadIdx.x; i < n; i += kSmallThreads) acc[i] = 0u;
+  small_scatter<IdxT, HOMO, ET>(acc, rows, n_rows, q * m / C, (q + 1) * m / C, indptr, indices, data, nnz, n,
+                                events);
+  cluster.sync();  // every CTA's accumulator is complete
+  const int64_t c0 = q * n / C, c1 = (q + 1) * n / C;
+  const float w0 = HOMO ? data[0] : 0.0f;
+  for (int64_t i = c0 + threadIdx.x; i < c1; i += kSmallThreads) {
+    if (HOMO) {
+      uint32_t s = 0;
+      for (int r = 0; r < C; ++r) s += cluster.map_shared_rank(acc, r)[i];
+      out[i] = (float)s * w0;
+    } else {
+      float s = 0.0f;
+      for (int r = 0; r < C; ++r) s += __uint_as_float(cluster.map_shared_rank(acc, r)[i]);
+      out[i] = s;
+    }
+  }
+  cluster.sync();  // no CTA leaves while another may still read its accumulator
 }
 
 // transpose=0, one warp per row.
@@ -387,54 +440,121 @@ bp_status compact_events(const void* events, bp_etype et, int64_t m, int32_t* li
   return BP_EINVAL;
 }
 
+constexpr int64_t kClusterSmallMaxM = 1 << 18;    // rows scanned by the cluster's CTAs
+constexpr int64_t kClusterSmallMaxNnz = 1 << 26;  // worst case: 2^22 shared adds per CTA at 16
+
+// Largest cluster (16, else 8) of the small-output kernel that can be resident, 0 if none.
+template <typename K>
+static int small_cluster_size(K kfn, size_t smem) {
+  for (int C : {16, 8}) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)C, 1, 1);
+    cfg.blockDim = dim3(kSmallThreads, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, kfn, &cfg) == cudaSuccess && clusters >= 1) return C;
+    cudaGetLastError();
+  }
+  return 0;
+}
+
 template <typename IdxT, bool HOMO, int ET>
 static bp_status launch_t_small(const IdxT* indptr, const IdxT* indices, const float* data, int64_t nnz, int64_t m,
-                                int64_t n, const void* events, float* out, cudaStream_t st) {
-  auto kfn = ecsr_t_small_kernel<IdxT, HOMO, ET>;
+                                int64_t n, const void* events, float* out, bool cluster, bool& done,
+                                cudaStream_t st) {
+  done = false;
   const size_t smem = small_smem_bytes(n);
-  if (smem > 48 * 1024) {
+  const size_t smem_max = small_smem_bytes(kSmallMaxN);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!cluster) {
+    auto kfn = ecsr_t_small_kernel<IdxT, HOMO, ET>;
     static bool configured[64] = {false};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev < 0 || dev >= 64) dev = 0;
-    if (!configured[dev]) {
-      BP_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)small_smem_bytes(kSmallMaxN)));
+    if (smem > 48 * 1024 && !configured[dev]) {
+      BP_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
       configured[dev] = true;
     }
+    {
+      ScopedKernelTimer tk(st);
+      kfn<<<1, kSmallThreads, smem, st>>>(indptr, indices, data, nnz, m, n, events, out);
+    }
+    done = true;
+    return check_launch("ecsr_t_small_kernel");
   }
+  auto kfn = ecsr_t_cluster_small_kernel<IdxT, HOMO, ET>;
+  static int csize[64] = {0};  // 0: not probed yet, -1: no cluster resident
+  if (csize[dev] == 0) {
+    BP_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max));
+    BP_CUDA_TRY(cudaFuncSetAttribute(kfn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    const int c = small_cluster_size(kfn, smem_max);
+    csize[dev] = c > 0 ? c : -1;
+  }
+  if (csize[dev] < 0) return BP_OK;  // not done: the caller takes the general path
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)csize[dev], 1, 1);
+  cfg.blockDim = dim3(kSmallThreads, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)csize[dev];
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
   {
     ScopedKernelTimer tk(st);
-    kfn<<<1, kSmallThreads, smem, st>>>(indptr, indices, data, nnz, m, n, events, out);
+    BP_CUDA_TRY(cudaLaunchKernelEx(&cfg, kfn, indptr, indices, data, nnz, m, n, events, out));
   }
-  return check_launch("ecsr_t_small_kernel");
+  done = true;
+  return check_launch("ecsr_t_cluster_small_kernel");
 }
 
 template <typename IdxT, bool HOMO>
 static bp_status ecsr_t_small(const IdxT* indptr, const IdxT* indices, const float* data, int64_t nnz, int64_t m,
-                              int64_t n, const void* events, bp_etype et, float* out, cudaStream_t st) {
+                              int64_t n, const void* events, bp_etype et, float* out, bool cluster, bool& done,
+                              cudaStream_t st) {
   switch (et) {
-    case BP_EV_BOOL: return launch_t_small<IdxT, HOMO, BP_EV_BOOL>(indptr, indices, data, nnz, m, n, events, out, st);
+    case BP_EV_BOOL:
+      return launch_t_small<IdxT, HOMO, BP_EV_BOOL>(indptr, indices, data, nnz, m, n, events, out, cluster, done, st);
     case BP_EV_F32_POS:
-      return launch_t_small<IdxT, HOMO, BP_EV_F32_POS>(indptr, indices, data, nnz, m, n, events, out, st);
+      return launch_t_small<IdxT, HOMO, BP_EV_F32_POS>(indptr, indices, data, nnz, m, n, events, out, cluster, done,
+                                                       st);
     case BP_EV_F32_NZ:
-      return launch_t_small<IdxT, HOMO, BP_EV_F32_NZ>(indptr, indices, data, nnz, m, n, events, out, st);
+      return launch_t_small<IdxT, HOMO, BP_EV_F32_NZ>(indptr, indices, data, nnz, m, n, events, out, cluster, done,
+                                                      st);
   }
   return BP_EINVAL;
 }
 
-// Whether a transposed product goes through the single-CTA kernel.
+// Whether a transposed product goes through the single-CTA kernel, or the one-cluster kernel.
 static bool t_small_fits(int64_t m, int64_t n, int64_t nnz) {
   return m <= kSmallMaxM && n <= kSmallMaxN && nnz <= kSmallMaxNnz;
+}
+static bool t_cluster_small_fits(int64_t m, int64_t n, int64_t nnz) {
+  return m <= kClusterSmallMaxM && n <= kSmallMaxN && nnz <= kClusterSmallMaxNnz;
 }
 
 template <typename IdxT>
 static bp_status ecsr_transpose_rowpar(const float* data, bool homo, const IdxT* indices, const IdxT* indptr,
                                        int64_t nnz, const void* events, bp_etype et, int64_t m, int64_t n,
                                        float* out, int32_t* list, int32_t* count, cudaStream_t st) {
-  if (t_small_fits(m, n, nnz))
-    return homo ? ecsr_t_small<IdxT, true>(indptr, indices, data, nnz, m, n, events, et, out, st)
-                : ecsr_t_small<IdxT, false>(indptr, indices, data, nnz, m, n, events, et, out, st);
+  const bool one = t_small_fits(m, n, nnz);
+  if (one || t_cluster_small_fits(m, n, nnz)) {
+    bool done = false;
+    const bp_status s0 = homo ? ecsr_t_small<IdxT, true>(indptr, indices, data, nnz, m, n, events, et, out, !one, done, st)
+                              : ecsr_t_small<IdxT, false>(indptr, indices, data, nnz, m, n, events, et, out, !one, done,
+                                                          st);
+    if (s0 != BP_OK || done) return s0;
+  }
   BP_CUDA_TRY(cudaMemsetAsync(count, 0, sizeof(int32_t), st));
   BP_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(float) * (size_t)n, st));
   bp_status s = compact_events(events, et, m, list, count, st);

@@ -102,13 +102,16 @@ def test_edge_cases(ev, orc):
     (20000, 3000, 20),    # several rounds of event scanning (4096 events a round)
     (5000, 49152, 100),   # the largest output held in shared memory
     (5000, 49153, 100),   # one column more: the general path
-    (600, 4000, 900),     # 540K entries: above the single-launch entry limit
+    (600, 4000, 900),     # 540K entries: the one-cluster kernel
+    (20000, 30000, 200),  # 4M entries, 20K rows: the one-cluster kernel
+    (270000, 2000, 4),    # more rows than the cluster scans: the general path
 ])
 def test_small_single_launch_path(ev, orc, m, n, k):
-  """The single-launch kernel of small transposed products (shared-memory accumulators)
-  and the general path on either side of its limits agree with the oracle: bit-exact
-  counts for a homogeneous weight, the FP64 bar for heterogeneous weights, every event
-  rule and both index types."""
+  """The single-launch kernels of transposed products with a small output (all columns in
+  shared memory: one CTA, or one cluster whose CTAs split the rows and sum through
+  distributed shared memory) and the general path on either side of their limits agree with
+  the oracle: bit-exact counts for a homogeneous weight, the FP64 bar for heterogeneous
+  weights, every event rule and both index types."""
   from brainpy_gb300.connect import fixed_prob_csr, normal_weights
   ind, ptr = fixed_prob_csr(m, n, k, seed=4)
   ind_h, ptr_h = ind.cpu().numpy(), ptr.cpu().numpy()

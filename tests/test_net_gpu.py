@@ -311,3 +311,23 @@ def test_grid_runner_matches_ops_path_across_calls(dyn):
   for k in ("V", "ge", "gi", "t_last", "spike"):
     assert torch.equal(getattr(a, k), getattr(b, k)), k
   assert int(cb.sum()) > 1000 and a.t_step == 200
+
+
+@pytest.mark.parametrize("n,n_exc", [(70_001, 56_000), (65_600, 65_600)])
+def test_grid_runner_odd_sizes(dyn, n, n_exc):
+  """Sizes whose last tile and last CTA are partly empty, and a network with no inhibitory
+  neuron: the grid runner equals the per-operator path, spike counts and state."""
+  fan = 300
+  ind_e, _ = dyn.fixed_prob_csr(n, n, fan, seed=n % 97)
+  ptr = torch.arange(n + 1, device="cuda", dtype=torch.int64) * fan
+  s = 80.0 / fan
+  V0 = _v0(n, seed=n % 89)
+  a = dyn.EINetwork(n, n_exc, indices=ind_e, indptr=ptr.to(torch.int32), we=0.6 * s, wi=6.7 * s, V0=V0)
+  b = dyn.EINetwork(n, n_exc, indices=ind_e, indptr=ptr.to(torch.int32), we=0.6 * s, wi=6.7 * s, V0=V0)
+  assert a.grid_eligible()
+  ca, _ = a.run(150, method="grid")
+  cb, _ = b.run(150, method="ops")
+  assert a.grid_error() == 0
+  assert torch.equal(ca, cb) and int(ca.sum()) > 0
+  for k in ("V", "ge", "gi", "t_last", "spike"):
+    assert torch.equal(getattr(a, k), getattr(b, k)), k

@@ -378,7 +378,7 @@ bp_status bp_net_run_grid(const bp_net_desc* desc, int32_t step0, int32_t steps,
   g.cnt = reinterpret_cast<int32_t*>(ws + L.off_cnt);
   g.list = reinterpret_cast<int32_t*>(ws + L.off_list);
   g.slice = L.slice;
-  BP_CUDA_TRY(cudaMemsetAsync(ws, 0, 16, st));  // barrier words and the error flag
+  BP_CUDA_TRY(cudaMemsetAsync(ws, 0, 8, st));  // barrier words (the error word is sticky)
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)L.ctas, 1, 1);
   cfg.blockDim = dim3(kGridThreads, 1, 1);

@@ -231,7 +231,7 @@ class EINetwork:
       L = _lib.lib()
       tw = int(L.bp_net_grid_tile(self.n))
       plan = _event.CSRPlan(self.indices, self.indptr, (self.n, self.n), tile_w=tw, cluster=1)
-      ws = _lib.workspace(L.bp_net_grid_workspace_size(self.n, tw), self.device)
+      ws = torch.zeros(max(int(L.bp_net_grid_workspace_size(self.n, tw)), 1), dtype=torch.uint8, device=self.device)
       self._grid = (plan, ws)
     return self._grid
 
@@ -244,8 +244,8 @@ class EINetwork:
     self.t_step += steps
 
   def grid_error(self):
-    """The grid runner's error word after its last run (0: every barrier wait ended); waits
-    for the run."""
+    """The grid runner's error word over every run of this network (0: every barrier wait
+    ended); waits for the runs."""
     if getattr(self, "_grid", None) is None:
       return 0
     err = ctypes.c_int32(0)

@@ -229,6 +229,8 @@ class Server:
       if j.stream is not None:
         torch.cuda.current_stream(self.device).wait_stream(j.stream)
       j.result = j.counts.cpu().numpy()  # the job's result on the host
+      if j.path == "grid" and j.net.grid_error():
+        raise RuntimeError(f"job {j.jid}: a grid-barrier wait of the whole-GPU runner ran out")
       j.finished_at = self.now()
       self.events += int(j.result.sum()) * self._fanout(j)
       self.active.remove(j)

@@ -385,7 +385,8 @@ bp_status bp_net_run(const bp_net_desc* descs_device, int32_t num_nets, int32_t 
  * counted separately; no column may have 65,536 or more incoming entries), updates the neurons
  * (dg = count * w, the LIF step of bp_lif_coba_step) and lists the new spikes, then waits on a
  * grid-wide barrier whose waits are bounded: a wait that runs out ends the launch early and
- * sets the error word that bp_net_grid_error reads.  Synaptic delays and rasters are not
+ * sets the error word (in the workspace, zeroed by the caller once) that bp_net_grid_error
+ * reads.  Synaptic delays and rasters are not
  * supported here (BP_ENOTSUP); desc is a host pointer.
  * ------------------------------------------------------------------------- */
 /* tile width for an n-neuron network, 0 when its clusters cannot all be resident at once */
@@ -393,7 +394,8 @@ int32_t bp_net_grid_tile(int64_t n);
 size_t bp_net_grid_workspace_size(int64_t n, int32_t tile_w);
 bp_status bp_net_run_grid(const bp_net_desc* desc, int32_t step0, int32_t steps, float dt, void* workspace,
                           size_t workspace_bytes, bp_stream_t stream);
-/* the error word of the last run on this workspace (0: every barrier wait ended); synchronises */
+/* the error word of the runs on this workspace since it was zeroed (0: every barrier wait
+ * ended; the caller zeroes a new workspace); synchronises */
 bp_status bp_net_grid_error(const void* workspace, int32_t* error, bp_stream_t stream);
 /* 1 when the last bp_net_run_grid launched with cooperative scheduling, 0 when the device refused
  * cooperative scheduling together with clusters and the launch went without it (every cluster

@@ -51,6 +51,17 @@ static size_t grid_smem_bytes(int tile_w) {
   return sizeof(uint32_t) * (size_t)(tile_w + kPlanPadSpan) + sizeof(int32_t) * (size_t)(kGridMaxCtas + 1);
 }
 
+constexpr int kGridMaxDelay = 64;  // spike-history slots (as the cluster runner)
+
+__device__ __forceinline__ int grid_pos_mod(int64_t a, int L) { return (int)(((a % L) + L) % L); }
+
+// bits of the 32 neurons from lo that are excitatory (global index < n_exc)
+__device__ __forceinline__ uint32_t grid_exc_bits(int64_t lo, int n_exc) {
+  if (lo + 32 <= n_exc) return 0xffffffffu;
+  if (lo >= n_exc) return 0u;
+  return (1u << (n_exc - lo)) - 1u;
+}
+
 // Bounded grid-wide barrier; returns false when the wait ran out.
 __device__ bool grid_barrier(const GridArgs& g, uint32_t nblocks, int* s_flag) {
   __threadfence();  // this thread's list / count writes before the arrival
@@ -86,7 +97,7 @@ __global__ void __launch_bounds__(kGridThreads, 1) net_grid_kernel(const bp_net_
                                                                    float dt, const GridArgs g) {
   constexpr unsigned FULL = 0xffffffffu;
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ int s_ok, s_flag, s_count, s_wsum[32];
+  __shared__ int s_ok, s_flag, s_count, s_nnew, s_wsum[32];
   cg::cluster_group cluster = cg::this_cluster();
   const int q = (int)cluster.block_rank();
   const int tile = (int)blockIdx.x / kGridR;
@@ -117,13 +128,36 @@ __global__ void __launch_bounds__(kGridThreads, 1) net_grid_kernel(const bp_net_
     if ((m >> lane) & 1u) my_list[pos + __popc(m & ((1u << lane) - 1u))] = (int32_t)(base + kw + lane);
   };
 
+  // Synaptic delays (VarDelay, brainpy/_src/delay.py:334-373): the excitatory rows propagate
+  // the spikes of step T - d_e, the inhibitory rows those of T - d_i (0: the previous step's
+  // spikes).  The spike bits of the last L steps stay in d.ring ([L][ceil(n/32)], step T in
+  // slot T mod L); this CTA's neurons are whole words of it (slice and base are multiples of
+  // 32), which only this CTA reads and writes.
+  const int L = (d.ring != nullptr && d.ring_len > 0) ? min((int)d.ring_len, kGridMaxDelay) : 0;
+  const int d_e = L ? max(0, min((int)d.delay_e, L)) : 0;
+  const int d_i = L ? max(0, min((int)d.delay_i, L)) : 0;
+  const int eff_e = max(d_e, 1), eff_i = max(d_i, 1);
+  const int64_t words = ((int64_t)d.n + 31) >> 5;
+  const int64_t word0 = base >> 5;
+  const int64_t T0 = (int64_t)step0 + d.step0;  // time index of this launch's first step
+  auto ring_word = [&](int slot, int k) -> uint32_t {  // word of neurons base + (k & ~31) ..
+    const int64_t w = word0 + (k >> 5);
+    return w < words ? __ldcg(d.ring + (int64_t)slot * words + w) : 0u;
+  };
+
   zero_acc();
-  // the initial list: this CTA's neurons that spiked in the step before the run
+  // the initial list: this CTA's neurons whose (delayed) spike the first step propagates
   if (tid == 0) s_count = 0;
   __syncthreads();
   for (int k0 = 0; k0 < slice; k0 += blockDim.x) {
     const int k = k0 + tid;
-    const unsigned m = __ballot_sync(FULL, k < nown && d.spike[base + k] != 0);
+    unsigned m = __ballot_sync(FULL, k < nown && d.spike[base + k] != 0);
+    if (L) {
+      const uint32_t em = grid_exc_bits(base + (k & ~31), d.n_exc);
+      const uint32_t me = d_e == 0 ? m : ring_word(grid_pos_mod(T0 - d_e, L), k);
+      const uint32_t mi = d_i == 0 ? m : ring_word(grid_pos_mod(T0 - d_i, L), k);
+      m = ((me & em) | (mi & ~em)) & __ballot_sync(FULL, k < nown);
+    }
     append(0, m, k0 + (tid & ~31));
   }
   __syncthreads();
@@ -131,6 +165,13 @@ __global__ void __launch_bounds__(kGridThreads, 1) net_grid_kernel(const bp_net_
   bool ok = grid_barrier(g, G, &s_flag);
 
   const int my_steps = d.step_limit > 0 ? min(steps, d.step_limit) : steps;
+  // history slots of step T (written) and of T + 1 - eff_e / eff_i (read for the next list)
+  int slot_w = 0, slot_e = 0, slot_i = 0;
+  if (L) {
+    slot_w = grid_pos_mod(T0, L);
+    slot_e = grid_pos_mod(T0 + 1 - eff_e, L);
+    slot_i = grid_pos_mod(T0 + 1 - eff_i, L);
+  }
   for (int s = 0; s < my_steps; ++s) {
     const int cur = s & 1, nxt = cur ^ 1;
     // leave together when any CTA of the cluster saw a grid-barrier wait run out
@@ -207,7 +248,10 @@ __global__ void __launch_bounds__(kGridThreads, 1) net_grid_kernel(const bp_net_
 
     // ---- 2. this CTA's neurons: sum the cluster's counters, update, list the spikes
     const float t = __fmul_rn((float)(step0 + d.step0 + s), dt);
-    if (tid == 0) s_count = 0;
+    if (tid == 0) {
+      s_count = 0;
+      s_nnew = 0;
+    }
     __syncthreads();
     for (int k0 = 0; k0 < slice; k0 += blockDim.x) {
       const int k = k0 + tid;
@@ -230,12 +274,27 @@ __global__ void __launch_bounds__(kGridThreads, 1) net_grid_kernel(const bp_net_
         if (d.v_trace && s < d.trace_steps) d.v_trace[(int64_t)s * d.n + i] = st.V;
       }
       const unsigned m = __ballot_sync(FULL, sp);
-      append(nxt, m, k0 + (tid & ~31));
+      if (lane == 0 && m) atomicAdd(&s_nnew, __popc(m));
+      unsigned ml = m;  // the rows the next step propagates
+      if (L) {
+        const int64_t w = word0 + (k >> 5);
+        if (lane == 0 && w < words) d.ring[(int64_t)slot_w * words + w] = m;
+        const uint32_t em = grid_exc_bits(base + (k & ~31), d.n_exc);
+        const uint32_t me = eff_e == 1 ? m : ring_word(slot_e, k);
+        const uint32_t mi = eff_i == 1 ? m : ring_word(slot_i, k);
+        ml = ((me & em) | (mi & ~em)) & __ballot_sync(FULL, k < nown);
+      }
+      append(nxt, ml, k0 + (tid & ~31));
     }
     __syncthreads();
     if (tid == 0) {
       g.cnt[(int64_t)nxt * G + blockIdx.x] = s_count;
-      if (d.spike_counts && s_count) atomicAdd(d.spike_counts + s, s_count);
+      if (d.spike_counts && s_nnew) atomicAdd(d.spike_counts + s, s_nnew);
+    }
+    if (L) {
+      slot_w = slot_w + 1 == L ? 0 : slot_w + 1;
+      slot_e = slot_e + 1 == L ? 0 : slot_e + 1;
+      slot_i = slot_i + 1 == L ? 0 : slot_i + 1;
     }
     cluster.sync();  // the cluster's reads of this CTA's counters are done
     zero_acc();
@@ -358,7 +417,9 @@ bp_status bp_net_run_grid(const bp_net_desc* desc, int32_t step0, int32_t steps,
              "net_run_grid: tile_w %d must be a positive multiple of %d", d.tile_w, kGridTileAlign);
   BP_REQUIRE((int64_t)d.n_tiles == ((int64_t)d.n + d.tile_w - 1) / d.tile_w, BP_EINVAL,
              "net_run_grid: n_tiles %d does not match n=%d, tile_w=%d", d.n_tiles, d.n, d.tile_w);
-  BP_REQUIRE(d.ring == nullptr || d.ring_len == 0, BP_ENOTSUP, "net_run_grid: synaptic delays are not supported");
+  BP_REQUIRE(d.ring_len >= 0 && d.ring_len <= kGridMaxDelay, BP_ENOTSUP,
+             "net_run_grid: %d delay steps exceed the %d the runner holds", d.ring_len, kGridMaxDelay);
+  BP_REQUIRE(d.ring_len == 0 || d.ring != nullptr, BP_EINVAL, "net_run_grid: null spike history");
   BP_REQUIRE(d.raster == nullptr, BP_ENOTSUP, "net_run_grid: rasters are not supported");
   BP_REQUIRE(d.seg_off && d.idx && d.V && d.ge && d.gi && d.t_last && d.spike, BP_EINVAL,
              "net_run_grid: null state or plan array");

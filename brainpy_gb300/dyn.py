@@ -210,10 +210,10 @@ class EINetwork:
   # ---- whole-GPU persistent form (networks larger than a cluster) ----------------------
   def grid_eligible(self):
     """Whether the network can run in one persistent launch over the GPU (bp_net_run_grid):
-    CSR connectivity, no synaptic delay, every tile's cluster resident at once, and no column
-    with 65,536 or more incoming entries (the runner counts excitatory and inhibitory events
-    in the two 16-bit halves of one word)."""
-    if self.jitconn is not None or self.ring is not None:
+    CSR connectivity, every tile's cluster resident at once, and no column with 65,536 or
+    more incoming entries (the runner counts excitatory and inhibitory events in the two
+    16-bit halves of one word)."""
+    if self.jitconn is not None:
       return False
     if _lib.lib().bp_net_grid_tile(self.n) <= 0:
       return False
@@ -226,8 +226,8 @@ class EINetwork:
     """The runner's plan (tiles of bp_net_grid_tile(n) columns) and workspace, built once."""
     if getattr(self, "_grid", None) is None:
       if not self.grid_eligible():
-        raise ValueError(f"network of {self.n} neurons cannot run on the grid runner (jitconn, delays, too many "
-                         "tiles for the resident clusters, or a column with 65,536 or more inputs)")
+        raise ValueError(f"network of {self.n} neurons cannot run on the grid runner (jitconn, too many tiles "
+                         "for the resident clusters, or a column with 65,536 or more inputs)")
       L = _lib.lib()
       tw = int(L.bp_net_grid_tile(self.n))
       plan = _event.CSRPlan(self.indices, self.indptr, (self.n, self.n), tile_w=tw, cluster=1)

@@ -386,8 +386,8 @@ bp_status bp_net_run(const bp_net_desc* descs_device, int32_t num_nets, int32_t 
  * (dg = count * w, the LIF step of bp_lif_coba_step) and lists the new spikes, then waits on a
  * grid-wide barrier whose waits are bounded: a wait that runs out ends the launch early and
  * sets the error word (in the workspace, zeroed by the caller once) that bp_net_grid_error
- * reads.  Synaptic delays and rasters are not
- * supported here (BP_ENOTSUP); desc is a host pointer.
+ * reads.  Synaptic delays work as in bp_net_run (the ring in desc); rasters are not supported
+ * (BP_ENOTSUP); desc is a host pointer.
  * ------------------------------------------------------------------------- */
 /* tile width for an n-neuron network, 0 when its clusters cannot all be resident at once */
 int32_t bp_net_grid_tile(int64_t n);

@@ -331,3 +331,24 @@ def test_grid_runner_odd_sizes(dyn, n, n_exc):
   assert torch.equal(ca, cb) and int(ca.sum()) > 0
   for k in ("V", "ge", "gi", "t_last", "spike"):
     assert torch.equal(getattr(a, k), getattr(b, k)), k
+
+
+def test_grid_runner_delays_match_ops_path(dyn):
+  """Synaptic delays on the grid runner (spike history in global memory, each CTA its own
+  words): 120,000 neurons, excitatory rows delayed 0.4 ms and inhibitory rows 0.9 ms, in two
+  runs of 90 steps, equal to one per-operator run of 180 steps: spike counts, state and the
+  history ring, bit for bit."""
+  n = 120_000
+  ne = int(0.8 * n)
+  s = 80.0 / (0.005 * n)
+  kw = dict(delay_e=0.4, delay_i=0.9)
+  a = dyn.EINetwork.fixed_prob(ne, n - ne, prob=0.005, we=0.6 * s, wi=6.7 * s, seed=17, V0=_v0(n, seed=18), **kw)
+  b = dyn.EINetwork(a.n, a.n_exc, indices=a.indices, indptr=a.indptr, we=a.we, wi=a.wi, V0=a.V.clone(), **kw)
+  assert a.grid_eligible() and a.ring is not None
+  c1, _ = a.run(90, method="grid")
+  c2, _ = a.run(90, method="grid")
+  cb, _ = b.run(180, method="ops")
+  assert a.grid_error() == 0
+  assert torch.equal(torch.cat([c1, c2]), cb) and int(cb.sum()) > 0
+  for k in ("V", "ge", "gi", "t_last", "spike", "ring"):
+    assert torch.equal(getattr(a, k), getattr(b, k)), k

@@ -322,7 +322,11 @@ static int grid_max_clusters(int tile_w) {
   if (dev < 0 || dev >= 64) dev = 0;
   if (cached[dev][0] == tile_w && cached[dev][1] > 0) return cached[dev][1];
   const size_t smem = grid_smem_bytes(tile_w);
-  if (cudaFuncSetAttribute(net_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+  // the attribute is the kernel's ceiling for every launch: the largest dynamic shared memory
+  // the device grants a block (launches then ask for their own tile's amount)
+  const size_t ceiling = (size_t)grid_smem_optin() - 1024;
+  if (smem > ceiling ||
+      cudaFuncSetAttribute(net_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ceiling) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }

@@ -128,22 +128,19 @@ __global__ void __launch_bounds__(256) jc_counts_to_out_kernel(float* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// Taichi GPU algorithm, push: warp per input column
+// Taichi GPU algorithm, push: warp per input column.  Event vectors: each warp examines 32
+// columns at a time (one event per lane, a ballot), then pushes the active ones one after
+// another with all 32 lanes; with sparse events the scan is a load per 32 columns instead of a
+// dependent load per column.  Homogeneous weights add equal values, so the order of the
+// atomic adds does not change the sums.
 // ---------------------------------------------------------------------------
 template <int KIND, int VK>
 __global__ void __launch_bounds__(256) jc_push_gpu_kernel(JcArgs a) {
   const int lane = threadIdx.x & 31;
   const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t gwarp = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const uint32_t lim = (uint32_t)a.num_row;
-  for (int64_t col = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); col < a.num_col; col += nwarps) {
-    float cv = 1.0f;
-    if (VK == VEC_EV_BOOL) {
-      if (!static_cast<const uint8_t*>(a.vec)[col]) continue;  // warp-uniform skip
-    } else if (VK == VEC_EV_F32) {
-      if (__ldg(static_cast<const float*>(a.vec) + col) == 0.0f) continue;
-    } else {
-      cv = __ldg(static_cast<const float*>(a.vec) + col);
-    }
+  auto push_column = [&](int64_t col, float cv) {
     const uint32_t i = (uint32_t)(col * 32 + lane);
     uint32_t r = a.step * (uint32_t)lane - 1u;
     uint32_t end = r + a.step;
@@ -157,6 +154,24 @@ __global__ void __launch_bounds__(256) jc_push_gpu_kernel(JcArgs a) {
       else add = w;  // event push kernels add the weight itself (_event_matvec_taichi.py:121, :250)
       atomicAdd(a.out + r, add);
       r += lfsr88_inc(key, a.fm);
+    }
+  };
+  if (VK == VEC_DENSE) {
+    for (int64_t col = gwarp; col < a.num_col; col += nwarps) push_column(col, __ldg(static_cast<const float*>(a.vec) + col));
+    return;
+  }
+  for (int64_t c0 = gwarp * 32; c0 < a.num_col; c0 += nwarps * 32) {
+    const int64_t mine = c0 + lane;
+    bool on = false;
+    if (mine < a.num_col) {
+      if (VK == VEC_EV_BOOL) on = static_cast<const uint8_t*>(a.vec)[mine] != 0;
+      else on = __ldg(static_cast<const float*>(a.vec) + mine) != 0.0f;
+    }
+    unsigned act = __ballot_sync(0xffffffffu, on);
+    while (act) {
+      const int b = __ffs(act) - 1;
+      act &= act - 1u;
+      push_column(c0 + b, 1.0f);
     }
   }
 }

@@ -85,6 +85,8 @@ SIGNATURES = {
     "bp_net_run_grid": (_c_i32, [_c_ptr, _c_i32, _c_i32, _c_f32, _c_ptr, _c_size, _c_ptr]),
     "bp_net_grid_error": (_c_i32, [_c_ptr, _c_ptr, _c_ptr]),
     "bp_net_grid_cooperative": (_c_i32, []),
+    "bp_net_grid_jit_workspace_size": (_c_size, [_c_i64]),
+    "bp_net_run_grid_jit": (_c_i32, [_c_ptr, _c_ptr, _c_i32, _c_i32, _c_i32, _c_f32, _c_ptr, _c_size, _c_ptr]),
     "bp_event_csrmv_noalloc_max_rows": (_c_i64, []),
     "bp_event_csrmv_noalloc": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_ptr, _c_i32, _c_i64,
                                         _c_i64, _c_i32, _c_ptr, _c_ptr]),

@@ -25,6 +25,7 @@
 #include <cooperative_groups.h>
 
 #include "common.cuh"
+#include "lfsr88.cuh"
 #include "lif.cuh"
 #include "plan.cuh"
 #include "timer.cuh"
@@ -38,6 +39,7 @@ constexpr int kGridThreads = 1024;
 constexpr int kGridTileAlign = 128;  // tile widths are multiples of this (R * 32)
 constexpr int kGridMaxCtas = 1024;   // one prefix element per thread
 constexpr unsigned kGridSpinLimit = 1u << 22;  // ~0.3-1 s of 64 ns sleeps
+constexpr int kGridUpd = 4;          // neurons a thread updates per round (jitconn runner)
 
 struct GridArgs {
   uint32_t* bar;    // [0] arrivals, [1] generation
@@ -277,8 +279,10 @@ __global__ void __launch_bounds__(kGridThreads, 1) net_grid_kernel(const bp_net_
       if (lane == 0 && m) atomicAdd(&s_nnew, __popc(m));
       unsigned ml = m;  // the rows the next step propagates
       if (L) {
+        // only this CTA's words: a warp past the slice (k0 rounds up to whole blocks of
+        // threads) would otherwise write over the next CTA's first words
         const int64_t w = word0 + (k >> 5);
-        if (lane == 0 && w < words) d.ring[(int64_t)slot_w * words + w] = m;
+        if (lane == 0 && (k & ~31) < slice && w < words) d.ring[(int64_t)slot_w * words + w] = m;
         const uint32_t em = grid_exc_bits(base + (k & ~31), d.n_exc);
         const uint32_t me = eff_e == 1 ? m : ring_word(slot_e, k);
         const uint32_t mi = eff_i == 1 ? m : ring_word(slot_i, k);
@@ -299,6 +303,183 @@ __global__ void __launch_bounds__(kGridThreads, 1) net_grid_kernel(const bp_net_
     cluster.sync();  // the cluster's reads of this CTA's counters are done
     zero_acc();
     ok = grid_barrier(g, G, &s_flag) && ok;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Just-in-time networks, push form (EventJitFPHomoLinear with atomic=True: outdim_parallel=False),
+// in one persistent launch: one CTA per SM owns a contiguous slice of neurons.  Step s:
+//   1. the spiking neurons of step s-1 (the CTAs' lists) are split over every warp of the grid;
+//      a warp regenerates a neuron's connections of both projections leaving its group, its 32
+//      lanes walking the 32 streams of the Taichi GPU push algorithm (the streams and the adds
+//      of jc_push_gpu_kernel: a homogeneous weight added once per connection with a float
+//      atomic into dge or dgi in global memory; equal addends, so the order of the adds does
+//      not change the sums and the result equals the per-operator path bit for bit);
+//   2. a grid barrier; every CTA reads and zeroes dge / dgi of its neurons and updates them,
+//      listing its spikes;
+//   3. a grid barrier.
+// The barrier and its bounded waits are those of the CSR runner; no clusters here, so a CTA
+// whose wait runs out records the error and leaves, and the others run out at their next
+// barrier.
+// ---------------------------------------------------------------------------
+struct JitGridArgs {
+  uint32_t* bar;
+  int32_t* err;
+  int32_t* cnt;    // [2][G]
+  int32_t* list;   // [2][G][slice]
+  float* dge;      // [n], zero between steps
+  float* dgi;      // [n]
+  int32_t slice;
+  uint32_t seed[4];          // E->E, E->I, I->E, I->I
+  uint32_t step_e, step_i;   // lane window of the projections onto E rows / onto I rows
+  FastMod fm;
+};
+
+__device__ __forceinline__ void jit_push(const JitGridArgs& g, uint32_t col, uint32_t seed, uint32_t nrow,
+                                         uint32_t step, float* out, float w, int lane) {
+  const uint32_t i = col * 32u + (uint32_t)lane;
+  uint32_t r = step * (uint32_t)lane - 1u;
+  uint32_t end = r + step;
+  if (nrow < end) end = nrow;
+  Lfsr88 key = lfsr88_key(seed + i);
+  r += lfsr88_inc(key, g.fm);
+  while (r < end) {
+    atomicAdd(out + r, w);
+    r += lfsr88_inc(key, g.fm);
+  }
+}
+
+__global__ void __launch_bounds__(kGridThreads, 1) net_grid_jit_kernel(const bp_net_desc d, int32_t step0,
+                                                                       int32_t steps, float dt, const JitGridArgs g) {
+  constexpr unsigned FULL = 0xffffffffu;
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_flag, s_count, s_wsum[32];
+  int* s_pre = reinterpret_cast<int*>(smem);  // G + 1
+  const uint32_t G = gridDim.x;
+  const int slice = g.slice;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const int64_t base = (int64_t)blockIdx.x * slice;
+  const int64_t rem = (int64_t)d.n - base;
+  const int nown = (int)(rem < 0 ? 0 : (rem > slice ? slice : rem));
+  const uint32_t ne = (uint32_t)d.n_exc, ni = (uint32_t)(d.n - d.n_exc);
+  GridArgs gb;  // the barrier words of the CSR runner's layout
+  gb.bar = g.bar;
+  gb.err = g.err;
+
+  auto append = [&](int par, unsigned m, int kw) {
+    int pos = 0;
+    if (lane == 0 && m) pos = atomicAdd(&s_count, __popc(m));
+    pos = __shfl_sync(FULL, pos, 0);
+    int32_t* my_list = g.list + ((int64_t)par * G + blockIdx.x) * slice;
+    if ((m >> lane) & 1u) my_list[pos + __popc(m & ((1u << lane) - 1u))] = (int32_t)(base + kw + lane);
+  };
+
+  if (tid == 0) s_count = 0;
+  __syncthreads();
+  for (int k0 = 0; k0 < slice; k0 += blockDim.x) {
+    const int k = k0 + tid;
+    const unsigned m = __ballot_sync(FULL, k < nown && d.spike[base + k] != 0);
+    append(0, m, k0 + (tid & ~31));
+  }
+  __syncthreads();
+  if (tid == 0) g.cnt[blockIdx.x] = s_count;
+  if (!grid_barrier(gb, G, &s_flag)) return;
+
+  const int my_steps = d.step_limit > 0 ? min(steps, d.step_limit) : steps;
+  for (int s = 0; s < my_steps; ++s) {
+    const int cur = s & 1, nxt = cur ^ 1;
+    // ---- 1. every spiking neuron of step s-1, this CTA's share, pushed by its warps
+    {
+      const int v = tid < (int)G ? __ldcg(g.cnt + (int64_t)cur * G + tid) : 0;
+      int incl = v;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+      }
+      if (lane == 31) s_wsum[warp] = incl;
+      __syncthreads();
+      if (warp == 0) {
+        const int t = lane < nwarps ? s_wsum[lane] : 0;
+        int ti = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int u = __shfl_up_sync(FULL, ti, o);
+          if (lane >= o) ti += u;
+        }
+        s_wsum[lane] = ti - t;
+      }
+      __syncthreads();
+      if (tid < (int)G) s_pre[tid] = s_wsum[warp] + incl - v;
+      if (tid == (int)G - 1) s_pre[G] = s_wsum[warp] + incl;
+      __syncthreads();
+    }
+    const int total = s_pre[G];
+    const int lo = (int)((int64_t)blockIdx.x * total / G), hi = (int)((int64_t)(blockIdx.x + 1) * total / G);
+    for (int p = lo + warp; p < hi; p += nwarps) {
+      int l = 0, h = (int)G;  // s_pre[l] <= p < s_pre[h]
+      while (h - l > 1) {
+        const int mid = (l + h) >> 1;
+        if (s_pre[mid] <= p) l = mid;
+        else h = mid;
+      }
+      const uint32_t j = (uint32_t)__ldcg(g.list + ((int64_t)cur * G + l) * slice + (p - s_pre[l]));
+      if (j < ne) {
+        jit_push(g, j, g.seed[0], ne, g.step_e, g.dge, d.we, lane);
+        jit_push(g, j, g.seed[1], ni, g.step_i, g.dge + ne, d.we, lane);
+      } else {
+        jit_push(g, j - ne, g.seed[2], ne, g.step_e, g.dgi, d.wi, lane);
+        jit_push(g, j - ne, g.seed[3], ni, g.step_i, g.dgi + ne, d.wi, lane);
+      }
+    }
+    if (!grid_barrier(gb, G, &s_flag)) return;  // every push of the step is in dge / dgi
+
+    // ---- 2. this CTA's neurons
+    const float t = __fmul_rn((float)(step0 + d.step0 + s), dt);
+    if (tid == 0) s_count = 0;
+    __syncthreads();
+    // kGridUpd neurons a thread per round, their loads issued before any update
+    for (int k00 = 0; k00 < slice; k00 += kGridUpd * kGridThreads) {
+      LifState st[kGridUpd];
+      float xe[kGridUpd], xi[kGridUpd];
+#pragma unroll
+      for (int u = 0; u < kGridUpd; ++u) {
+        const int k = k00 + u * kGridThreads + tid;
+        xe[u] = xi[u] = 0.0f;
+        if (k < nown) {
+          const int64_t i = base + k;
+          xe[u] = __ldcg(g.dge + i);
+          xi[u] = __ldcg(g.dgi + i);
+          st[u] = LifState{d.V[i], d.ge[i], d.gi[i], d.t_last[i]};
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kGridUpd; ++u) {
+        const int k0 = k00 + u * kGridThreads;
+        const int k = k0 + tid;
+        bool sp = false;
+        if (k < nown) {
+          const int64_t i = base + k;
+          g.dge[i] = 0.0f;
+          g.dgi[i] = 0.0f;
+          sp = lif_coba_update(d.p, st[u], xe[u], xi[u], t, dt);
+          d.V[i] = st[u].V;
+          d.ge[i] = st[u].ge;
+          d.gi[i] = st[u].gi;
+          d.t_last[i] = st[u].t_last;
+          d.spike[i] = sp ? 1 : 0;
+          if (d.v_trace && s < d.trace_steps) d.v_trace[(int64_t)s * d.n + i] = st[u].V;
+        }
+        const unsigned m = __ballot_sync(FULL, sp);
+        append(nxt, m, k0 + (tid & ~31));
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      g.cnt[(int64_t)nxt * G + blockIdx.x] = s_count;
+      if (d.spike_counts && s_count) atomicAdd(d.spike_counts + s, s_count);
+    }
+    if (!grid_barrier(gb, G, &s_flag)) return;
   }
 }
 
@@ -367,6 +548,25 @@ static GridLayout grid_layout(int64_t n, int32_t tile_w) {
   return L;
 }
 
+struct JitLayout {
+  size_t off_cnt, off_list, off_dge, off_dgi, bytes;
+  int ctas, slice;
+};
+
+static JitLayout jit_layout(int64_t n) {
+  JitLayout L{};
+  L.ctas = std::min(device_sm_count(), kGridMaxCtas);
+  int64_t slice = (n + L.ctas - 1) / L.ctas;
+  slice = (slice + 31) / 32 * 32;
+  L.slice = (int)std::max<int64_t>(slice, 32);
+  L.off_cnt = 256;
+  L.off_list = L.off_cnt + align_up(sizeof(int32_t) * 2 * (size_t)L.ctas, 256);
+  L.off_dge = L.off_list + align_up(sizeof(int32_t) * 2 * (size_t)L.ctas * (size_t)L.slice, 256);
+  L.off_dgi = L.off_dge + align_up(sizeof(float) * (size_t)n, 256);
+  L.bytes = L.off_dgi + align_up(sizeof(float) * (size_t)n, 256);
+  return L;
+}
+
 }  // namespace bp
 
 using namespace bp;
@@ -405,6 +605,71 @@ bp_status bp_net_grid_error(const void* workspace, int32_t* error, bp_stream_t s
   BP_CUDA_TRY(cudaMemcpyAsync(error, static_cast<const char*>(workspace) + 8, sizeof(int32_t), cudaMemcpyDeviceToHost,
                               as_cuda(stream)));
   BP_CUDA_TRY(cudaStreamSynchronize(as_cuda(stream)));
+  return BP_OK;
+}
+
+size_t bp_net_grid_jit_workspace_size(int64_t n) {
+  if (n <= 0) return 0;
+  return jit_layout(n).bytes;
+}
+
+bp_status bp_net_run_grid_jit(const bp_net_desc* desc, const uint32_t* seeds, int32_t clen, int32_t step0,
+                              int32_t steps, float dt, void* workspace, size_t workspace_bytes, bp_stream_t stream) {
+  clear_error();
+  cudaStream_t st = as_cuda(stream);
+  BP_REQUIRE(desc != nullptr && seeds != nullptr, BP_EINVAL, "net_run_grid_jit: null descriptor or seeds");
+  const bp_net_desc& d = *desc;
+  BP_REQUIRE(steps >= 0, BP_EINVAL, "net_run_grid_jit: negative steps");
+  BP_REQUIRE(d.n > 0 && d.n_exc >= 0 && d.n_exc <= d.n, BP_EINVAL, "net_run_grid_jit: bad sizes n=%d n_exc=%d", d.n,
+             d.n_exc);
+  BP_REQUIRE((int64_t)d.n * 32 < INT32_MAX, BP_ENOTSUP,
+             "net_run_grid_jit: %d neurons exceed the reference's int32 stream indexing", d.n);
+  BP_REQUIRE(clen >= 1, BP_EINVAL, "net_run_grid_jit: conn_len must be >= 1 (got %d)", clen);
+  BP_REQUIRE(d.ring == nullptr || d.ring_len == 0, BP_ENOTSUP, "net_run_grid_jit: synaptic delays are not supported");
+  BP_REQUIRE(d.raster == nullptr, BP_ENOTSUP, "net_run_grid_jit: rasters are not supported");
+  BP_REQUIRE(d.V && d.ge && d.gi && d.t_last && d.spike, BP_EINVAL, "net_run_grid_jit: null state array");
+  const JitLayout L = jit_layout(d.n);
+  BP_REQUIRE(workspace && workspace_bytes >= L.bytes, BP_ENOMEM, "net_run_grid_jit: workspace %zu < %zu",
+             workspace_bytes, L.bytes);
+  if (steps == 0) return BP_OK;
+  static bool configured[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!configured[dev]) {
+    int per_sm = 0;
+    BP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, net_grid_jit_kernel, kGridThreads,
+                                                              sizeof(int32_t) * (kGridMaxCtas + 1)));
+    BP_REQUIRE(per_sm >= 1, BP_ENOTSUP, "net_run_grid_jit: the kernel cannot be resident");
+    configured[dev] = true;
+  }
+  char* ws = static_cast<char*>(workspace);
+  JitGridArgs g;
+  g.bar = reinterpret_cast<uint32_t*>(ws);
+  g.err = reinterpret_cast<int32_t*>(ws + 8);
+  g.cnt = reinterpret_cast<int32_t*>(ws + L.off_cnt);
+  g.list = reinterpret_cast<int32_t*>(ws + L.off_list);
+  g.dge = reinterpret_cast<float*>(ws + L.off_dge);
+  g.dgi = reinterpret_cast<float*>(ws + L.off_dgi);
+  g.slice = L.slice;
+  for (int k = 0; k < 4; ++k) g.seed[k] = seeds[k];
+  const int32_t sh_e = (d.n_exc + 1) >> 5, sh_i = ((d.n - d.n_exc) + 1) >> 5;
+  g.step_e = (uint32_t)(sh_e > 1 ? sh_e : 1);
+  g.step_i = (uint32_t)(sh_i > 1 ? sh_i : 1);
+  g.fm = make_fastmod((uint32_t)clen);
+  BP_CUDA_TRY(cudaMemsetAsync(ws, 0, 8, st));  // barrier words (the error word is sticky)
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)L.ctas, 1, 1);
+  cfg.blockDim = dim3(kGridThreads, 1, 1);
+  cfg.dynamicSmemBytes = sizeof(int32_t) * (size_t)(L.ctas + 1);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  ScopedKernelTimer tk(st);
+  BP_CUDA_TRY(cudaLaunchKernelEx(&cfg, net_grid_jit_kernel, d, step0, steps, dt, g));
   return BP_OK;
 }
 

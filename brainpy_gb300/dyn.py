@@ -209,12 +209,14 @@ class EINetwork:
 
   # ---- whole-GPU persistent form (networks larger than a cluster) ----------------------
   def grid_eligible(self):
-    """Whether the network can run in one persistent launch over the GPU (bp_net_run_grid):
-    CSR connectivity, every tile's cluster resident at once, and no column with 65,536 or
-    more incoming entries (the runner counts excitatory and inhibitory events in the two
-    16-bit halves of one word)."""
+    """Whether the network can run in one persistent launch over the GPU: CSR connectivity
+    (bp_net_run_grid) with every tile's cluster resident at once and no column with 65,536
+    or more incoming entries (the runner counts excitatory and inhibitory events in the two
+    16-bit halves of one word); or just-in-time connectivity in the push form
+    (outdim_parallel=False; bp_net_run_grid_jit) without delays."""
     if self.jitconn is not None:
-      return False
+      return (not bool(self.jitconn.get("outdim_parallel", True)) and self.ring is None
+              and self.n * 32 < 2 ** 31)
     if _lib.lib().bp_net_grid_tile(self.n) <= 0:
       return False
     if not hasattr(self, "_indeg_ok"):
@@ -223,7 +225,14 @@ class EINetwork:
     return self._indeg_ok
 
   def _grid_state(self):
-    """The runner's plan (tiles of bp_net_grid_tile(n) columns) and workspace, built once."""
+    """The runner's plan (tiles of bp_net_grid_tile(n) columns) and workspace, built once
+    (just-in-time networks: the workspace only)."""
+    if getattr(self, "_grid", None) is None and self.jitconn is not None:
+      if not self.grid_eligible():
+        raise ValueError("the whole-GPU runner takes just-in-time networks in the push form (outdim_parallel="
+                         "False) without delays")
+      nb = int(_lib.lib().bp_net_grid_jit_workspace_size(self.n))
+      self._grid = (None, torch.zeros(max(nb, 1), dtype=torch.uint8, device=self.device))
     if getattr(self, "_grid", None) is None:
       if not self.grid_eligible():
         raise ValueError(f"network of {self.n} neurons cannot run on the grid runner (jitconn, too many tiles "
@@ -237,11 +246,34 @@ class EINetwork:
 
   def _run_grid(self, steps, dt, counts, trace, trace_steps):
     plan, ws = self._grid_state()
+    if self.jitconn is not None:
+      d = self._state_desc(counts, trace, trace_steps)
+      seeds = (ctypes.c_uint32 * 4)(*[_jitconn._seed(x, False) for x in self.jitconn["seeds"]])
+      st = _lib.lib().bp_net_run_grid_jit(ctypes.byref(d), seeds, _jitconn.conn_len(self.jitconn["prob"]), 0,
+                                          int(steps), float(dt), _lib.ptr(ws), ws.numel(),
+                                          _lib.stream_handle(self.device))
+      _lib.check(st, "net_run_grid_jit")
+      self.t_step += steps
+      return
     d = self.descriptor(counts, None, trace, trace_steps, 0, plan=plan)
     st = _lib.lib().bp_net_run_grid(ctypes.byref(d), 0, int(steps), float(dt), _lib.ptr(ws), ws.numel(),
                                     _lib.stream_handle(self.device))
     _lib.check(st, "net_run_grid")
     self.t_step += steps
+
+  def _state_desc(self, spike_counts=None, v_trace=None, trace_steps=0):
+    """A descriptor of the state and parameters only (no connectivity plan)."""
+    d = _lib.NetDesc()
+    d.n, d.n_exc = self.n, self.n_exc
+    d.we, d.wi = self.we, self.wi
+    d.p = self.params.c()
+    d.V, d.ge, d.gi, d.t_last = (self.V.data_ptr(), self.ge.data_ptr(), self.gi.data_ptr(), self.t_last.data_ptr())
+    d.spike = self.spike.data_ptr()
+    d.spike_counts = spike_counts.data_ptr() if spike_counts is not None else None
+    d.v_trace = v_trace.data_ptr() if v_trace is not None else None
+    d.trace_steps = int(trace_steps)
+    d.step0 = int(self.t_step)
+    return d
 
   def grid_error(self):
     """The grid runner's error word over every run of this network (0: every barrier wait

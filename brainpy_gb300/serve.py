@@ -172,6 +172,8 @@ class Server:
         job.path = "cluster"
         job.net._cluster_plan()
       elif job.conn == "csr" and job.net.grid_eligible():
+        # jitconn jobs stay on their per-operator graphs: those overlap with the other jobs'
+        # kernels on side streams, where a whole-GPU launch holds every SM while it spins
         job.path = "grid"
         job.net._grid_state()
       else:

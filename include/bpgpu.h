@@ -397,6 +397,16 @@ bp_status bp_net_run_grid(const bp_net_desc* desc, int32_t step0, int32_t steps,
 /* the error word of the runs on this workspace since it was zeroed (0: every barrier wait
  * ended; the caller zeroes a new workspace); synchronises */
 bp_status bp_net_grid_error(const void* workspace, int32_t* error, bp_stream_t stream);
+/* A just-in-time network in the push form (the four EventJitFPHomoLinear projections with
+ * atomic=True, i.e. jitconn.event_mv_prob_homo with outdim_parallel=False, Taichi GPU streams) in
+ * one persistent cooperative launch, one CTA per SM: each step regenerates the spiking neurons'
+ * connections (seeds: E->E, E->I, I->E, I->I; clen = conn_len(prob)) and adds the weight of every
+ * connection with a float atomic, as the per-operator path does, so the results are equal bit for
+ * bit.  desc's plan fields are unused; no delays, no raster.  The error word is read by
+ * bp_net_grid_error on this workspace. */
+size_t bp_net_grid_jit_workspace_size(int64_t n);
+bp_status bp_net_run_grid_jit(const bp_net_desc* desc, const uint32_t* seeds, int32_t clen, int32_t step0,
+                              int32_t steps, float dt, void* workspace, size_t workspace_bytes, bp_stream_t stream);
 /* 1 when the last bp_net_run_grid launched with cooperative scheduling, 0 when the device refused
  * cooperative scheduling together with clusters and the launch went without it (every cluster
  * was checked to be resident at once), -1 before the first launch */

@@ -352,3 +352,25 @@ def test_grid_runner_delays_match_ops_path(dyn):
   assert torch.equal(torch.cat([c1, c2]), cb) and int(cb.sum()) > 0
   for k in ("V", "ge", "gi", "t_last", "spike", "ring"):
     assert torch.equal(getattr(a, k), getattr(b, k)), k
+
+
+@pytest.mark.parametrize("n", [50_000, 400_000])
+def test_grid_runner_jitconn_push_matches_ops_path(dyn, n):
+  """A just-in-time network in the push form (outdim_parallel=False, the served jitconn jobs)
+  on the whole-GPU runner, in two runs, equal to the per-operator path (event_mv_prob_homo
+  push per projection) bit for bit: spike counts of every step and the final state."""
+  ne = int(0.8 * n)
+  fan = 1000
+  jit = dict(prob=fan / n, seeds=(21, 22, 23, 24), outdim_parallel=False)
+  s = 80.0 / fan
+  V0 = _v0(n, seed=31)
+  a = dyn.EINetwork(n, ne, jitconn=jit, we=0.6 * s, wi=6.7 * s, V0=V0)
+  b = dyn.EINetwork(n, ne, jitconn=jit, we=0.6 * s, wi=6.7 * s, V0=V0)
+  assert a.grid_eligible() and not a.fits_cluster()
+  c1, _ = a.run(60)  # method "cluster" takes the whole-GPU runner for this network
+  c2, _ = a.run(60, method="grid")
+  cb, _ = b.run(120, method="ops")
+  assert a.grid_error() == 0
+  assert torch.equal(torch.cat([c1, c2]), cb) and int(cb.sum()) > 0
+  for k in ("V", "ge", "gi", "t_last", "spike"):
+    assert torch.equal(getattr(a, k), getattr(b, k)), k

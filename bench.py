@@ -426,9 +426,9 @@ def main():
 
 
 def north_star_forms(args):
-  """The batched and served forms, the COBA example and the 4M-neuron jitconn network, each
-  timed with CUDA events under its own clock record, summarised beside the headline operator
-  line."""
+  """The batched and served forms, the COBA example, the 4M-neuron jitconn network and a 1M-
+  neuron CSR network on the whole-GPU runner, each timed with CUDA events under its own clock
+  record, summarised beside the headline operator line."""
   import copy
   out = {}
   a = copy.copy(args)
@@ -465,6 +465,8 @@ def north_star_forms(args):
       "ms_per_step": r["ms_per_step"], "connections_generated_per_s": r["connections_generated_per_s"],
       "synaptic_events_per_s": r["synaptic_events_per_s"], "firing_rate_hz": r["firing_rate_hz"],
       "clocks": r["clocks"]}
+  torch.cuda.empty_cache()
+  out["large_network"] = bench_large_network()
   torch.cuda.empty_cache()
   from brainpy_gb300 import serve
   a = copy.copy(args)
@@ -646,6 +648,32 @@ def bench_batched(args):
           "form": "tuned tiles; every network's 5000 steps in one CUDA graph launch holding one persistent "
                   "kernel per cluster size as concurrent branches",
           "clocks": clk, "gpu_launches": batch.launches}
+
+
+def bench_large_network(n=1_000_000, steps=1000):
+  """A CSR network larger than one thread-block cluster (1M neurons, 80/20, fan-out 1000, COBA
+  weights scaled by 80/1000): the whole-GPU persistent runner (one launch for the run) against
+  the per-operator path replayed from CUDA graphs of 50 steps, from the same state; spike
+  counts compared step by step."""
+  from brainpy_gb300 import dyn
+  ne = int(0.8 * n)
+  prob = 1000 / n
+  V0 = np.random.default_rng(12).normal(-55.0, 5.0, n).astype(np.float32)
+  a = dyn.EINetwork.fixed_prob(ne, n - ne, prob=prob, we=0.6 * 0.08, wi=6.7 * 0.08, seed=12, V0=V0)
+  b = dyn.EINetwork(a.n, a.n_exc, indices=a.indices, indptr=a.indptr, we=a.we, wi=a.wi, V0=a.V.clone())
+  ca = torch.zeros(steps + 50, dtype=torch.int32, device="cuda")
+  cb = torch.zeros(steps + 50, dtype=torch.int32, device="cuda")
+  a.run(50, method="grid", spike_counts=ca[:50])  # plan, workspace, module load
+  b.run(50, method="ops", graph_steps=50, spike_counts=cb[:50])
+  clocks = ClockSampler(torch.cuda.current_device())
+  t_grid, _ = _cuda_time(lambda: a.run(steps, method="grid", spike_counts=ca[50:]))
+  clk = clocks.stop()
+  t_ops, _ = _cuda_time(lambda: b.run(steps, method="ops", graph_steps=50, spike_counts=cb[50:]))
+  return {"config": f"{n} neurons 80/20, FixedProb fan-out 1000, {steps} steps after 50",
+          "grid_runner_steps_per_s": steps / t_grid, "per_op_graph_steps_per_s": steps / t_ops,
+          "speedup": t_ops / t_grid, "same_spike_counts": bool(torch.equal(ca, cb)),
+          "barrier_waits_ran_out": bool(a.grid_error()),
+          "firing_rate_hz": float(ca[50:].double().sum()) / n / (steps * 1e-4), "clocks": clk}
 
 
 def bench_jitconn_net(args):

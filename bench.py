@@ -464,7 +464,7 @@ def north_star_forms(args):
       "config": r["config"]["workload"] + f", {r['steps']} steps timed", "steps_per_s": r["value"],
       "ms_per_step": r["ms_per_step"], "connections_generated_per_s": r["connections_generated_per_s"],
       "synaptic_events_per_s": r["synaptic_events_per_s"], "firing_rate_hz": r["firing_rate_hz"],
-      "clocks": r["clocks"]}
+      "push_form": r["push_form"], "clocks": r["clocks"]}
   torch.cuda.empty_cache()
   out["large_network"] = bench_large_network()
   torch.cuda.empty_cache()
@@ -696,13 +696,28 @@ def bench_jitconn_net(args):
   t, _ = _cuda_time(lambda: net.run(steps, method="ops", graph_steps=50, spike_counts=counts[60:]))
   clk = clocks.stop()
   n_spk = int(counts[60:].sum())
+  del net
+  torch.cuda.empty_cache()
+  # the same network built with the projections' other form (EventJitFPHomoLinear(atomic=True):
+  # outdim_parallel=False, an equally distributed realisation of the connectivity), whose
+  # step regenerates only the spiking neurons' connections, on the whole-GPU runner
+  push = dyn.EINetwork(n, ne, jitconn=dict(prob=p, seeds=(11, 12, 13, 14), outdim_parallel=False), we=0.6,
+                       wi=6.7 * 0.08, V0=V0)
+  pc = torch.zeros(steps + 60, dtype=torch.int32, device="cuda")
+  push.run(60, method="grid", spike_counts=pc[:60])
+  t_push, _ = _cuda_time(lambda: push.run(steps, method="grid", spike_counts=pc[60:]))
+  p_spk = int(pc[60:].sum())
+  push_form = {"steps_per_s": steps / t_push, "ms_per_step": t_push / steps * 1e3,
+               "firing_rate_hz": p_spk / n / (steps * 1e-4), "synaptic_events_per_s": p_spk * 1000 / t_push,
+               "barrier_waits_ran_out": bool(push.grid_error()),
+               "form": "outdim_parallel=False (atomic=True), whole-GPU persistent runner, one launch"}
   return {"metric": "network-steps/s (4M-neuron jitconn E/I network)", "value": steps / t, "unit": "steps/s",
           "n_gpus": 1, "steps": steps, "warmup": 60, "ms_per_step": t / steps * 1e3, "higher_is_better": True,
           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
           "config": {"workload": "4M neurons 80/20, fan-in 1000 via event_mv_prob_homo (outdim_parallel=True), "
                                  "we=0.6 wi=0.536 (COBA's we, its wi x 80/1000: ~2 % firing a step)"},
           "synaptic_events_per_s": n_spk * 1000 / t, "connections_generated_per_s": 4e9 / (t / steps),
-          "firing_rate_hz": n_spk / n / (steps * 1e-4), "clocks": clk}
+          "firing_rate_hz": n_spk / n / (steps * 1e-4), "push_form": push_form, "clocks": clk}
 
 
 def bench_serve(args):

@@ -188,14 +188,16 @@ __global__ void __launch_bounds__(256) compact_blocked_kernel(const void* __rest
 //   kWeight heterogeneous weights, events: float32 sum of w_ij
 //   kRowVal homogeneous weight, dense vector x: float32 sum of x_i, out = w * sum
 //   kWRow   heterogeneous weights, dense vector x: float32 sum of w_ij * x_i
-enum { kCount = 0, kWeight = 1, kRowVal = 2, kWRow = 3 };
+//   kFix    heterogeneous weights held as int32 fixed point (w * 2^k, a fixed-weight plan),
+//           events: exact integer sums, out = (float)sum * 2^-k
+enum { kCount = 0, kWeight = 1, kRowVal = 2, kWRow = 3, kFix = 4 };
 
 // Threads of a tiled CTA: 1024 (64 registers a thread), except the per-synapse-weight modes
 // with two chunk rounds, whose double-buffered 48-byte chunks need more than 64 registers:
 // 768 threads (80 registers) there.
 template <int MODE, int RND>
 constexpr int tiled_threads() {
-  return ((MODE == kWeight || MODE == kWRow) && RND >= 2) ? 768 : kTiledThreads;
+  return ((MODE == kWeight || MODE == kWRow || MODE == kFix) && RND >= 2) ? 768 : kTiledThreads;
 }
 
 // Shared-memory reductions issued under a predicate (no branch): entries with index >= lim
@@ -225,6 +227,7 @@ __device__ __forceinline__ void accumulate8(uint32_t acc_s, uint4 v, float4 w0, 
     // and contended float adds to shared memory cost far more than the predicate saves
     // (measured: 77 us against 60 us per call at N = 1e6, fan-out 1000, 2 % events).
     if (MODE == kCount) asm volatile("red.shared.add.u32 [%0], 1;" ::"r"(ad));
+    else if (MODE == kFix) asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(ad), "r"(__float_as_uint(ww[q])));
     else if (MODE == kWeight) red_if(x[q], lim, ad, ww[q]);
     else if (MODE == kRowVal) red_if(x[q], lim, ad, xv);
     else red_if(x[q], lim, ad, __fmul_rn(ww[q], xv));
@@ -245,6 +248,7 @@ struct TiledArgs {
   const int32_t* counts;
   const float* w_homo;
   const float* row_val;  // dense vector for kRowVal / kWRow
+  const uint32_t* meta;  // plan meta ([2]: the fixed-point exponent of kFix)
   float* out;
   int64_t m, n;  // a batch of vectors: row_val rows of m, out rows of n
   int32_t tile_w, n_tiles, nb, acc_words;
@@ -263,7 +267,7 @@ struct TiledArgs {
 // segment is longer than RND * G chunks also prefetches its next chunk into L1 with the unit.
 template <int MODE, int G, int RND, bool PF, bool BATCH>
 __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_kernel(const TiledArgs a) {
-  constexpr bool HAS_W = (MODE == kWeight || MODE == kWRow);
+  constexpr bool HAS_W = (MODE == kWeight || MODE == kWRow || MODE == kFix);
   constexpr bool HAS_X = (MODE == kRowVal || MODE == kWRow);
   constexpr unsigned FULL = 0xffffffffu;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -393,9 +397,13 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
           const bool in = c < U.ln[u];
           U.lim[u][r] = in ? tile_w : 0u;
           const uint64_t e = 8ull * (U.st[u] + (in ? c : 0u));
-          if (MODE == kCount) U.vv[u][r] = in ? ld_stream_u4(a.idx + e) : lane_pads;
+          if (MODE == kCount || MODE == kFix) U.vv[u][r] = in ? ld_stream_u4(a.idx + e) : lane_pads;
           else U.vv[u][r] = ld_stream_u4(a.idx + e);
-          if (HAS_W) {
+          if (MODE == kFix) {  // integer weights: pads and idle lanes add 0 to the spare words
+            const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            U.w0[u][r] = in ? ld_stream_f4(a.w + e) : z;
+            U.w1[u][r] = in ? ld_stream_f4(a.w + e + 4) : z;
+          } else if (HAS_W) {
             U.w0[u][r] = ld_stream_f4(a.w + e);
             U.w1[u][r] = ld_stream_f4(a.w + e + 4);
           }
@@ -471,7 +479,7 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
     for (int r = 0; r < 8; ++r)
       if (r < R) x[r] = *reinterpret_cast<const uint4*>(cluster.map_shared_rank(acc, r) + c);
     float o[4];
-    if (MODE == kCount) {
+    if (MODE == kCount || MODE == kFix) {
       uint4 s = make_uint4(0, 0, 0, 0);
 #pragma unroll
       for (int r = 0; r < 8; ++r) {
@@ -482,10 +490,18 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
           s.w += x[r].w;
         }
       }
-      o[0] = (float)s.x * w;
-      o[1] = (float)s.y * w;
-      o[2] = (float)s.z * w;
-      o[3] = (float)s.w * w;
+      if (MODE == kFix) {  // two's-complement sums; 2^-k is exact
+        const float sc = __int_as_float((127 - (int)__ldg(a.meta + 2)) << 23);
+        o[0] = __fmul_rn((float)(int32_t)s.x, sc);
+        o[1] = __fmul_rn((float)(int32_t)s.y, sc);
+        o[2] = __fmul_rn((float)(int32_t)s.z, sc);
+        o[3] = __fmul_rn((float)(int32_t)s.w, sc);
+      } else {
+        o[0] = (float)s.x * w;
+        o[1] = (float)s.y * w;
+        o[2] = (float)s.z * w;
+        o[3] = (float)s.w * w;
+      }
     } else {
       float4 s = make_float4(0, 0, 0, 0);
 #pragma unroll
@@ -1062,7 +1078,7 @@ static void tiled_config(double chunks, bool has_w, int32_t variant, int& G, int
 template <int MODE>
 static bp_status launch_tiled(const TiledArgs& a, int R, double chunks, cudaStream_t st) {
   int G, RND, PF;
-  tiled_config(chunks, MODE == kWeight || MODE == kWRow, a.variant, G, RND, PF);
+  tiled_config(chunks, MODE == kWeight || MODE == kWRow || MODE == kFix, a.variant, G, RND, PF);
 #define BP_TILED_CASE(g, r)                                                                           \
   if (G == g && RND == r) {                                                                           \
     if (a.batch > 1) return launch_tiled_g<MODE, g, r, false, true>(a, R, st);                        \
@@ -1211,6 +1227,7 @@ static bp_status tiled_args_from_plan(const bp_csr_plan* plan, int cluster, Tile
   a.seg_off = v.seg_off;
   a.idx = v.idx;
   a.w = v.w;
+  a.meta = v.meta;
   a.batch = 1;
   a.variant = plan->variant;
   a.m = plan->m;
@@ -1389,9 +1406,39 @@ namespace bp {
 // One launch pair for `batch` vectors: vectors (events or dense values) are rows of m, outputs
 // rows of n, both contiguous.  `dense` selects sparse.csrmv semantics (vec != 0 rows carry their
 // value) over event semantics.
+// The entries of a fixed-weight plan whose weights are too small for the fixed point, by row
+// (row r's are [ptr[r], ptr[r + 1])), added in float by fix_side_kernel after the tiles.
+struct FixSide {
+  const int32_t* ptr;
+  const int32_t* cols;
+  const float* w;
+  int64_t count;
+};
+
+// One warp per compaction block: the active rows' small-weight entries, float atomics into out.
+__global__ void __launch_bounds__(256) fix_side_kernel(const int32_t* __restrict__ lists,
+                                                       const int32_t* __restrict__ counts, int nb, FixSide side,
+                                                       int64_t n, float* __restrict__ out) {
+  cudaGridDependencySynchronize();  // the tiles of this call have written out
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (int)(gridDim.x * (blockDim.x >> 5));
+  for (int b = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); b < nb; b += nwarps) {
+    const int cnt = counts[b];
+    for (int j = lane; j < cnt; j += 32) {
+      const int32_t row = lists[(int64_t)b * kCompactRows + j];
+      const int32_t e0 = __ldg(side.ptr + row), e1 = __ldg(side.ptr + row + 1);
+      for (int32_t e = e0; e < e1; ++e) {
+        const int32_t c = __ldg(side.cols + e);
+        if ((uint32_t)c < (uint64_t)n) atomicAdd(out + c, __ldg(side.w + e));
+      }
+    }
+  }
+}
+
 static bp_status planned_batch(const char* who, const bp_csr_plan* plan, const float* w_homo, const void* vec,
                                bp_etype etype, bool dense, int32_t batch, float* out, int32_t cluster,
-                               void* workspace, size_t workspace_bytes, cudaStream_t st) {
+                               void* workspace, size_t workspace_bytes, cudaStream_t st,
+                               const FixSide* side = nullptr) {
   BP_REQUIRE(plan != nullptr && plan->mem != nullptr, BP_EINVAL, "%s: null plan", who);
   BP_REQUIRE(etype >= BP_EV_BOOL && etype <= BP_EV_F32_NZ, BP_EDTYPE, "%s: bad event type %d", who, (int)etype);
   BP_REQUIRE(batch >= 0 && batch <= 65535, BP_EINVAL, "%s: batch must be in [0, 65535] (got %d)", who, batch);
@@ -1410,6 +1457,12 @@ static bp_status planned_batch(const char* who, const bp_csr_plan* plan, const f
   BP_REQUIRE(!homo || w_homo != nullptr, BP_EINVAL, "%s: homogeneous plan needs w_homo", who);
   const size_t need = bp_event_csrmv_planned_batch_workspace_size(plan, batch);
   BP_REQUIRE(workspace && workspace_bytes >= need, BP_ENOMEM, "%s: workspace %zu < %zu", who, workspace_bytes, need);
+  const bool fixed = plan->kind == 2;
+  BP_REQUIRE(!fixed || (side != nullptr && plan->heter != 0), BP_EINVAL,
+             "%s: a fixed-weight plan runs through bp_event_csrmv_planned_fixed", who);
+  BP_REQUIRE(fixed || side == nullptr, BP_EINVAL, "%s: not a fixed-weight plan", who);
+  BP_REQUIRE(!fixed || (!dense && batch == 1), BP_ENOTSUP,
+             "%s: a fixed-weight plan serves one event vector a call", who);
   if (is_split_plan(plan)) {
     BP_REQUIRE(plan->heter == 0 && plan->tile_w % 64 == 0 && plan->tile_w <= kSplitMaxTile &&
                    split_smem_bytes(plan->tile_w) <= (size_t)max_smem_optin() - kStaticSmemReserve,
@@ -1438,8 +1491,61 @@ static bp_status planned_batch(const char* who, const bp_csr_plan* plan, const f
   a.batch = batch;
   a.vec_out = ((reinterpret_cast<uintptr_t>(out) & 15u) == 0 && (batch == 1 || (n & 3) == 0)) ? 1 : 0;
   if (dense) return homo ? launch_tiled<kRowVal>(a, cluster, chunks, st) : launch_tiled<kWRow>(a, cluster, chunks, st);
+  if (fixed) {
+    s = launch_tiled<kFix>(a, cluster, chunks, st);
+    if (s != BP_OK || side->count == 0) return s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    const int blocks = std::max(1, std::min((a.nb + 7) / 8, device_sm_count() * 4));
+    cfg.gridDim = dim3((unsigned)blocks, 1, 1);
+    cfg.blockDim = dim3(256, 1, 1);
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    BP_CUDA_TRY(cudaLaunchKernelEx(&cfg, fix_side_kernel, (const int32_t*)lists, (const int32_t*)counts, (int)a.nb,
+                                   *side, (int64_t)n, out));
+    return check_launch("fix_side_kernel");
+  }
   return homo ? launch_tiled<kCount>(a, cluster, chunks, st) : launch_tiled<kWeight>(a, cluster, chunks, st);
 }
+
+// Converts a heterogeneous plan's float weights to int32 fixed point, q = rint(w * 2^k), in place
+// (convert != 0), and lists the nonzero weights with |w| < tau, which the fixed point cannot carry
+// within the accuracy bar, as (row, column, w) at side[0 .. count) (up to cap of them; the count
+// is always complete).  One warp per row.
+__global__ void __launch_bounds__(256) fix_weights_kernel(const uint32_t* __restrict__ seg_off,
+                                                          const uint16_t* __restrict__ idx, float* w, int64_t m,
+                                                          int tile_w, int n_tiles, float scale_up, float tau,
+                                                          int32_t* side_rows, int32_t* side_cols, float* side_w,
+                                                          int64_t cap, unsigned long long* count, int convert) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < m; r += nwarps) {
+    const uint32_t* so = seg_off + r * (int64_t)(n_tiles + 1);
+    for (int t = 0; t < n_tiles; ++t) {
+      const uint64_t e0 = 8ull * so[t], e1 = 8ull * so[t + 1];
+      for (uint64_t e = e0 + lane; e < e1; e += 32) {
+        const uint32_t x = idx[e];
+        if (x >= (uint32_t)tile_w) continue;  // padding: weight 0 stays 0
+        const float v = w[e];
+        const bool small = v != 0.0f && fabsf(v) < tau;
+        if (small) {
+          const unsigned long long pos = atomicAdd(count, 1ull);
+          if ((int64_t)pos < cap) {
+            side_rows[pos] = (int32_t)r;
+            side_cols[pos] = (int32_t)((int64_t)t * tile_w + x);
+            side_w[pos] = v;
+          }
+        }
+        if (convert) w[e] = __int_as_float(small ? 0 : __float2int_rn(v * scale_up));
+      }
+    }
+  }
+}
+
+__global__ void set_word_kernel(uint32_t* p, uint32_t v) { *p = v; }
 
 }  // namespace bp
 
@@ -1540,6 +1646,49 @@ int32_t bp_csr_plan_count_tile(int64_t n) {
 
 extern "C" {
 
+bp_status bp_csr_plan_fix_weights(bp_csr_plan* plan, int32_t k, float tau, int32_t* side_rows, int32_t* side_cols,
+                                  float* side_w, int64_t side_cap, uint64_t* side_count, int32_t convert,
+                                  bp_stream_t stream) {
+  clear_error();
+  cudaStream_t st = as_cuda(stream);
+  BP_REQUIRE(plan != nullptr && plan->mem != nullptr, BP_EINVAL, "csr_plan_fix_weights: null plan");
+  BP_REQUIRE(plan->heter != 0 && plan->kind == 0, BP_EINVAL,
+             "csr_plan_fix_weights: needs a general heterogeneous plan (heter=%d, kind=%d)", plan->heter, plan->kind);
+  BP_REQUIRE(k >= 0 && k <= 100, BP_EINVAL, "csr_plan_fix_weights: exponent %d outside [0, 100]", k);
+  BP_REQUIRE(side_count != nullptr, BP_EINVAL, "csr_plan_fix_weights: null side count");
+  BP_REQUIRE(side_cap <= 0 || (side_rows && side_cols && side_w), BP_EINVAL, "csr_plan_fix_weights: null side arrays");
+  PlanView v = plan_view(plan);
+  BP_CUDA_TRY(cudaMemsetAsync(side_count, 0, sizeof(uint64_t), st));
+  if (plan->m > 0) {
+    const int64_t g = std::min<int64_t>((plan->m + 7) / 8, (int64_t)device_sm_count() * 16);
+    fix_weights_kernel<<<(unsigned)g, 256, 0, st>>>(v.seg_off, v.idx, const_cast<float*>(v.w), plan->m, plan->tile_w,
+                                                  plan->n_tiles, ldexpf(1.0f, k), tau, side_rows, side_cols, side_w,
+                                                  side_cap, reinterpret_cast<unsigned long long*>(side_count),
+                                                  convert);
+    bp_status s = check_launch("fix_weights_kernel");
+    if (s != BP_OK) return s;
+  }
+  if (convert) {
+    set_word_kernel<<<1, 1, 0, st>>>(const_cast<uint32_t*>(v.meta) + 2, (uint32_t)k);
+    bp_status s = check_launch("set_word_kernel");
+    if (s != BP_OK) return s;
+    plan->kind = 2;
+  }
+  return BP_OK;
+}
+
+bp_status bp_event_csrmv_planned_fixed(const bp_csr_plan* plan, const int32_t* side_ptr, const int32_t* side_cols,
+                                       const float* side_w, int64_t side_count, const void* events, bp_etype etype,
+                                       float* out, int32_t cluster, void* workspace, size_t workspace_bytes,
+                                       bp_stream_t stream) {
+  clear_error();
+  BP_REQUIRE(side_count >= 0 && (side_count == 0 || (side_ptr && side_cols && side_w)), BP_EINVAL,
+             "event_csrmv_planned_fixed: null side arrays for %lld entries", (long long)side_count);
+  FixSide side{side_ptr, side_cols, side_w, side_count};
+  return planned_batch("event_csrmv_planned_fixed", plan, nullptr, events, etype, false, 1, out, cluster, workspace,
+                       workspace_bytes, as_cuda(stream), &side);
+}
+
 bp_status bp_event_csrmv_planned(const bp_csr_plan* plan, const float* w_homo, const void* events, bp_etype etype,
                                  float* out, int32_t cluster, void* workspace, size_t workspace_bytes,
                                  bp_stream_t stream) {
@@ -1576,6 +1725,7 @@ bp_status bp_csrmv_planned_n(const bp_csr_plan* plan, const float* w_homo, const
   clear_error();
   cudaStream_t st = as_cuda(stream);
   BP_REQUIRE(plan != nullptr && plan->mem != nullptr, BP_EINVAL, "csrmv_planned_n: null plan");
+  BP_REQUIRE(plan->kind == 0, BP_EINVAL, "csrmv_planned_n: needs a general plan (kind %d)", plan->kind);
   const int64_t m = plan->m, n = plan->n;
   if (m == 0) return BP_OK;
   BP_REQUIRE(out != nullptr, BP_EINVAL, "csrmv_planned_n: null out");

@@ -17,9 +17,11 @@
 //                               [seg_off[r][t], seg_off[r][t+1]) of idx (8 entries each)
 //   idx[entries]        uint16
 //   w[entries]          float32 (heterogeneous plans only)
-//   meta[2]             uint32  meta[0] != 0 when no row holds a column twice (checked for rows of
+//   meta[4]             uint32  meta[0] != 0 when no row holds a column twice (checked for rows of
 //                               up to kPlanDupCheckMax entries, longer rows count as not checked
-//                               and clear it); meta[1] = the longest row's length
+//                               and clear it); meta[1] = the longest row's length; meta[2] = the
+//                               fixed-point exponent k of a fixed-weight plan (weights stored as
+//                               int32 w * 2^k), written by bp_csr_plan_fix_weights
 // Row r's chunks start at entry align8(indptr[r]) + (8*T + 8) * r, a bound that needs no
 // prefix sum (row r needs at most nnz_r + 7*T padded entries and the gap to row r + 1 is at
 // least nnz_r + 8*T + 1).  Chunk indices are 32-bit: a plan holds fewer than 2^32 chunks.

@@ -6,6 +6,7 @@ brainpy/_src/math/event/_csr_matvec_taichi.py:344-452 (csrmv_taichi) and
 brainpy/_src/math/event/_info_collection.py:24-43 (info).
 """
 import ctypes
+import math
 import os
 import weakref
 from typing import Optional, Tuple, Union
@@ -37,15 +38,18 @@ class CSRPlan:
     m, n = self.shape
     L = _lib.lib()
     heter = data is not None and data.numel() > 1
-    if kind not in ("general", "count"):
-      raise ValueError(f"plan kind must be 'general' or 'count', got {kind!r}")
+    if kind not in ("general", "count", "fixed"):
+      raise ValueError(f"plan kind must be 'general', 'count' or 'fixed', got {kind!r}")
+    if kind == "fixed" and not heter:
+      raise ValueError("a fixed-weight plan needs per-synapse weights")
     # "count": tiles of up to 65,472 columns with 16-bit counters and per-tile partial counts
     # (event products with a homogeneous weight, one vector a call); "general": tiles whose
     # 32-bit accumulator fits one CTA (every product, batches, weights)
     if kind == "count" and tile_w is None and not heter:
       tile_w = L.bp_csr_plan_count_tile(n) or None
     if tile_w is None:
-      kind = "general"
+      if kind == "count":
+        kind = "general"  # too few columns for a counting tile
       tile_w = L.bp_csr_plan_default_tile(n, self.cluster)
       if tile_w <= 0:
         raise _lib.BPError("bp_csr_plan_default_tile failed: " + L.bp_last_error().decode())
@@ -63,6 +67,9 @@ class CSRPlan:
       self.c.kind = 1
     self.heter = bool(heter)
     self.device = dev
+    self.side = None
+    if kind == "fixed":
+      self._fix_weights(data, indices, n)
     # per-call state kept ready: the C plan struct, a unit weight, and one workspace per stream
     # (calls on one stream are ordered, so they can share it)
     self._L = L
@@ -70,6 +77,38 @@ class CSRPlan:
     self._one = torch.ones(1, dtype=torch.float32, device=dev)
     self._ws_bytes = L.bp_event_csrmv_planned_workspace_size(self._cref)
     self._ws = {}
+
+  def _fix_weights(self, data, indices, n):
+    """Fixed-point weights: k from the largest column sum of |w| (no column's sum times 2^k
+    reaches 2^31 - 2^24), tau = 2^-(k+1) / 5e-6; the weights below tau go to the side list,
+    sorted by row."""
+    L = _lib.lib()
+    dev = self.device
+    colsum = torch.zeros(max(n, 1), dtype=torch.float64, device=dev)
+    colsum.index_add_(0, indices.to(torch.int64), data.abs().to(torch.float64))
+    bound = float(colsum.max()) if colsum.numel() else 0.0
+    k = 30 if bound <= 0.0 else int(math.floor(math.log2((2.0 ** 31 - 2.0 ** 24) / bound)))
+    k = max(0, min(k, 100))
+    tau = float(2.0 ** -(k + 1) / 5e-6)
+    cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+    sp = _lib.stream_handle(dev)
+    _lib.check(L.bp_csr_plan_fix_weights(ctypes.byref(self.c), k, tau, None, None, None, 0, _lib.ptr(cnt), 0, sp),
+               "csr_plan_fix_weights")
+    count = int(cnt.item())
+    rows = torch.empty(max(count, 1), dtype=torch.int32, device=dev)
+    cols = torch.empty(max(count, 1), dtype=torch.int32, device=dev)
+    ws = torch.empty(max(count, 1), dtype=torch.float32, device=dev)
+    _lib.check(L.bp_csr_plan_fix_weights(ctypes.byref(self.c), k, tau, _lib.ptr(rows), _lib.ptr(cols), _lib.ptr(ws),
+                                         count, _lib.ptr(cnt), 1, sp), "csr_plan_fix_weights")
+    m = self.shape[0]
+    order = torch.argsort(rows[:count].to(torch.int64), stable=True)
+    rows, cols, ws = rows[:count][order], cols[:count][order], ws[:count][order]
+    ptr = torch.zeros(m + 1, dtype=torch.int32, device=dev)
+    if count:
+      ptr[1:] = torch.cumsum(torch.bincount(rows.to(torch.int64), minlength=m), 0).to(torch.int32)
+    self.side = (ptr, cols.contiguous(), ws.contiguous(), count)
+    self.fix_exponent, self.fix_tau = k, tau
+    self.kind = "fixed"
 
   def _workspace(self, stream_ptr, nbytes=None):
     nbytes = self._ws_bytes if nbytes is None else nbytes
@@ -91,6 +130,14 @@ class CSRPlan:
     if not self.heter:
       w = (data if data is not None else self._one).data_ptr()
     sp = _lib.raw_stream(self.device)
+    if self.side is not None:
+      ptr, cols, ws, count = self.side
+      st = self._L.bp_event_csrmv_planned_fixed(self._cref, ptr.data_ptr(), cols.data_ptr(), ws.data_ptr(), count,
+                                                ev.data_ptr(), etype, out.data_ptr(), self.cluster,
+                                                self._workspace(sp).data_ptr(), self._ws_bytes, sp)
+      if st:
+        _lib.check(st, "event_csrmv_planned_fixed")
+      return out
     st = self._L.bp_event_csrmv_planned(self._cref, w, ev.data_ptr(), etype, out.data_ptr(), self.cluster,
                                         self._workspace(sp).data_ptr(), self._ws_bytes, sp)
     if st:
@@ -248,6 +295,9 @@ _PLAN_DISABLE = os.environ.get("BPGPU_DISABLE_PLAN", "0") == "1"
 # (BPGPU_SPLIT_MIN_N; off unless set: the autotuner times it against the general plan and
 # routes a matrix to it when it wins)
 _SPLIT_MIN_N = int(os.environ.get("BPGPU_SPLIT_MIN_N", 1 << 62))
+# per-synapse weights take the fixed-point plan whenever the plan path is taken (N = 1e6,
+# fan-out 1000, 2 %: 51.4 against 61.1 us a call); BPGPU_FIXED_MIN_N raises the threshold
+_FIXED_MIN_N = int(os.environ.get("BPGPU_FIXED_MIN_N", 0))
 
 
 def _ident(t):
@@ -279,7 +329,7 @@ def _set_route(data, indices, indptr, shape, route):
 
 
 def _route(data, indices, indptr, shape):
-  """The autotuned kernel family of this matrix: "row", "tiled", "split", or None (not tuned,
+  """The autotuned kernel family of this matrix: "row", "tiled", "split", "fixed", or None (not tuned,
   or the arrays changed since)."""
   if not _ROUTES:
     return None
@@ -296,8 +346,14 @@ def _route(data, indices, indptr, shape):
 
 def _plan_kind(data, n, route):
   """Plan kind of an event product: "count" (split plan) for a homogeneous weight on many
-  columns, unless the autotuner chose the general plan; "general" otherwise."""
-  if data.numel() > 1 or route == "tiled":
+  columns, unless the autotuner chose the general plan; "fixed" (fixed-point weights) for
+  per-synapse weights unless the autotuner chose the general plan (or the matrix has fewer
+  than BPGPU_FIXED_MIN_N columns); "general" otherwise."""
+  if data.numel() > 1:
+    if route == "fixed" or (route is None and int(n) >= _FIXED_MIN_N):
+      return "fixed"
+    return "general"
+  if route == "tiled":
     return "general"
   if route == "split":
     return "count"
@@ -333,7 +389,9 @@ def _cached_plan(data, indices, indptr, shape, force=False, routed=True, kind="g
     if route is None and (n < _PLAN_MIN_N or indices.numel() < _PLAN_MIN_NNZ):
       return None
   heter = data.numel() > 1
-  if heter:
+  if heter and kind == "count":
+    kind = "general"
+  if not heter and kind == "fixed":
     kind = "general"
   key = (_matrix_key(data, indices, indptr, m, n), kind)
   ver = _versions(data, indices, indptr)
@@ -354,12 +412,12 @@ def _plan_for(data, indices, indptr, shape):
   """The plan the transposed event product of this matrix runs on (autotuned route first,
   then the size thresholds), or None for the plain CSR kernels."""
   route = _route(data, indices, indptr, shape)
-  return _cached_plan(data, indices, indptr, shape, force=route in ("tiled", "split"),
+  return _cached_plan(data, indices, indptr, shape, force=route in ("tiled", "split", "fixed"),
                       kind=_plan_kind(data, shape[1], route))
 
 
 def _valid_choice(choice):
-  if choice in ("row", "split"):
+  if choice in ("row", "split", "fixed"):
     return True
   if not isinstance(choice, str) or not choice.startswith("tiled:"):
     return False
@@ -423,6 +481,9 @@ def autotune(data, indices, indptr, events, *, shape: Tuple[int, int], transpose
       if not heter and _lib.lib().bp_csr_plan_count_tile(n) > 0:
         split = _cached_plan(d, indices, indptr, (m, n), force=True, kind="count")
         cands["split"] = lambda: split.csrmv(events, d, out=out, float_rule=float_rule)
+      if heter:
+        fixed = _cached_plan(d, indices, indptr, (m, n), force=True, kind="fixed")
+        cands["fixed"] = lambda: fixed.csrmv(events, None, out=out, float_rule=float_rule)
     best, times = tuning.pick(cands, timer or tuning.cuda_timer(reps))
     rec = {"choice": best, "times_us": times, "rate": rate}
     cache.store(key, rec)
@@ -432,14 +493,17 @@ def autotune(data, indices, indptr, events, *, shape: Tuple[int, int], transpose
   route = choice.split(":", 1)[0]
   _set_route(d, indices, indptr, (m, n), route)
   # keep only the plan the chosen family runs on: each holds about 2.6 bytes per stored entry
-  for kind in ("general", "count"):
-    if route == "row" or (route == "split") != (kind == "count"):
+  keep = {"tiled": "general", "split": "count", "fixed": "fixed"}.get(route)
+  for kind in ("general", "count", "fixed"):
+    if kind != keep:
       _PLANS.pop((mkey, kind), None)
   if route == "tiled":
     plan = _cached_plan(d, indices, indptr, (m, n), force=True)
     plan.variant = int(choice.split(":", 1)[1])
   elif route == "split":
     _cached_plan(d, indices, indptr, (m, n), force=True, kind="count")
+  elif route == "fixed":
+    _cached_plan(d, indices, indptr, (m, n), force=True, kind="fixed")
   return rec
 
 

@@ -203,7 +203,8 @@ typedef struct {
   int32_t kind;       /* 0: general plan (cluster kernels; every product, batches, weights);
                          1: counting plan (split kernels; homogeneous weight, one event vector a
                          call; tile_w from bp_csr_plan_count_tile).  bp_csr_plan_build sets 0; the
-                         caller sets 1 on a homogeneous plan built with a counting tile. */
+                         caller sets 1 on a homogeneous plan built with a counting tile;
+                         2: fixed-weight plan (set by bp_csr_plan_fix_weights). */
 } bp_csr_plan;
 
 /* tile width the tiled kernels run best with on the current device for n columns and
@@ -235,6 +236,24 @@ bp_status bp_csr_plan_build(const float* data, int64_t ndata, const void* indice
  * idx[entries], w[entries] or NULL */
 bp_status bp_csr_plan_arrays(const bp_csr_plan* plan, const uint32_t** seg_off, const uint16_t** idx,
                              const float** w);
+
+/* Fixed-weight plans (bp_csr_plan.kind = 2; event.csrmv transpose with per-synapse weights, one
+ * event vector a call).  bp_csr_plan_fix_weights converts a general heterogeneous plan's weights in
+ * place to int32 fixed point q = rint(w * 2^k) (the caller picks k so that no column's sum of |w|
+ * times 2^k reaches 2^31) and lists the nonzero weights with |w| < tau as (row, column, w) in
+ * side_rows / side_cols / side_w (up to side_cap of them; *side_count, a device word, receives the
+ * full count).  With convert = 0 it only counts them.  The caller sorts the listed entries by row
+ * into side_ptr[m + 1] / side_cols / side_w for bp_event_csrmv_planned_fixed, which adds the fixed-
+ * point weights with exact integer shared-memory adds (out = (float)sum * 2^-k) and then the listed
+ * weights with float atomics.  With tau = 2^-(k+1) / 5e-6 every fixed-point term is within 5e-6
+ * of its weight, relative, so a sum stays within 1e-5 of the exact sum of its terms' magnitudes. */
+bp_status bp_csr_plan_fix_weights(bp_csr_plan* plan, int32_t k, float tau, int32_t* side_rows, int32_t* side_cols,
+                                  float* side_w, int64_t side_cap, uint64_t* side_count, int32_t convert,
+                                  bp_stream_t stream);
+bp_status bp_event_csrmv_planned_fixed(const bp_csr_plan* plan, const int32_t* side_ptr, const int32_t* side_cols,
+                                       const float* side_w, int64_t side_count, const void* events, bp_etype etype,
+                                       float* out, int32_t cluster, void* workspace, size_t workspace_bytes,
+                                       bp_stream_t stream);
 
 /* event.csrmv, transpose=1, on a plan: out (n) = sum of the active rows.  `w_homo` is the
  * homogeneous weight (device pointer to one float) for homogeneous plans and is ignored for

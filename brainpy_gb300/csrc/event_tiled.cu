@@ -249,6 +249,7 @@ struct TiledArgs {
   const float* w_homo;
   const float* row_val;  // dense vector for kRowVal / kWRow
   const uint32_t* meta;  // plan meta ([2]: the fixed-point exponent of kFix)
+  const uint4* fx;       // kFix: chunk c's 8 indices and 8 integer weights at fx[3c .. 3c + 2]
   float* out;
   int64_t m, n;  // a batch of vectors: row_val rows of m, out rows of n
   int32_t tile_w, n_tiles, nb, acc_words;
@@ -397,13 +398,20 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
           const bool in = c < U.ln[u];
           U.lim[u][r] = in ? tile_w : 0u;
           const uint64_t e = 8ull * (U.st[u] + (in ? c : 0u));
-          if (MODE == kCount || MODE == kFix) U.vv[u][r] = in ? ld_stream_u4(a.idx + e) : lane_pads;
-          else U.vv[u][r] = ld_stream_u4(a.idx + e);
-          if (MODE == kFix) {  // integer weights: pads and idle lanes add 0 to the spare words
+          if (MODE == kFix) {
+            // one 48-byte record a chunk (indices, then integer weights): one read a segment;
+            // pads and idle lanes add 0 to the spare words
+            const uint4* fp = a.fx + 3ull * (U.st[u] + (in ? c : 0u));
             const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            U.w0[u][r] = in ? ld_stream_f4(a.w + e) : z;
-            U.w1[u][r] = in ? ld_stream_f4(a.w + e + 4) : z;
-          } else if (HAS_W) {
+            U.vv[u][r] = in ? __ldcs(fp) : lane_pads;
+            U.w0[u][r] = in ? __ldcs(reinterpret_cast<const float4*>(fp + 1)) : z;
+            U.w1[u][r] = in ? __ldcs(reinterpret_cast<const float4*>(fp + 2)) : z;
+          } else if (MODE == kCount) {
+            U.vv[u][r] = in ? ld_stream_u4(a.idx + e) : lane_pads;
+          } else {
+            U.vv[u][r] = ld_stream_u4(a.idx + e);
+          }
+          if (HAS_W && MODE != kFix) {
             U.w0[u][r] = ld_stream_f4(a.w + e);
             U.w1[u][r] = ld_stream_f4(a.w + e + 4);
           }
@@ -432,11 +440,19 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
       for (int u = 0; u < UB; ++u) {
         for (uint32_t c = gl + RND * G; c < U.ln[u]; c += G) {
           const uint64_t e = 8ull * (U.st[u] + c);
-          const uint4 x = ld_stream_u4(a.idx + e);
+          uint4 x;
           float4 y0 = make_float4(0, 0, 0, 0), y1 = y0;
-          if (HAS_W) {
-            y0 = ld_stream_f4(a.w + e);
-            y1 = ld_stream_f4(a.w + e + 4);
+          if (MODE == kFix) {
+            const uint4* fp = a.fx + 3ull * (U.st[u] + c);
+            x = __ldcs(fp);
+            y0 = __ldcs(reinterpret_cast<const float4*>(fp + 1));
+            y1 = __ldcs(reinterpret_cast<const float4*>(fp + 2));
+          } else {
+            x = ld_stream_u4(a.idx + e);
+            if (HAS_W) {
+              y0 = ld_stream_f4(a.w + e);
+              y1 = ld_stream_f4(a.w + e + 4);
+            }
           }
           accumulate8<MODE>(acc_s, x, y0, y1, U.xs[u], tile_w);
         }
@@ -1413,6 +1429,7 @@ struct FixSide {
   const int32_t* cols;
   const float* w;
   int64_t count;
+  const uint4* fx;  // the plan's chunks as 48-byte records (bp_csr_plan_fix_interleave)
 };
 
 // One warp per compaction block: the active rows' small-weight entries, float atomics into out.
@@ -1492,6 +1509,7 @@ static bp_status planned_batch(const char* who, const bp_csr_plan* plan, const f
   a.vec_out = ((reinterpret_cast<uintptr_t>(out) & 15u) == 0 && (batch == 1 || (n & 3) == 0)) ? 1 : 0;
   if (dense) return homo ? launch_tiled<kRowVal>(a, cluster, chunks, st) : launch_tiled<kWRow>(a, cluster, chunks, st);
   if (fixed) {
+    a.fx = side->fx;
     s = launch_tiled<kFix>(a, cluster, chunks, st);
     if (s != BP_OK || side->count == 0) return s;
     cudaLaunchAttribute attr[1];
@@ -1546,6 +1564,18 @@ __global__ void __launch_bounds__(256) fix_weights_kernel(const uint32_t* __rest
 }
 
 __global__ void set_word_kernel(uint32_t* p, uint32_t v) { *p = v; }
+
+// chunk c of a plan -> fx[3c] = its 8 indices, fx[3c + 1 .. 3c + 2] = its 8 (integer) weights
+__global__ void __launch_bounds__(256) fix_interleave_kernel(const uint4* __restrict__ idx,
+                                                             const uint4* __restrict__ w, uint4* __restrict__ fx,
+                                                             uint64_t nchunks) {
+  for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < nchunks;
+       c += (uint64_t)gridDim.x * blockDim.x) {
+    fx[3 * c] = idx[c];
+    fx[3 * c + 1] = w[2 * c];
+    fx[3 * c + 2] = w[2 * c + 1];
+  }
+}
 
 }  // namespace bp
 
@@ -1677,14 +1707,38 @@ bp_status bp_csr_plan_fix_weights(bp_csr_plan* plan, int32_t k, float tau, int32
   return BP_OK;
 }
 
-bp_status bp_event_csrmv_planned_fixed(const bp_csr_plan* plan, const int32_t* side_ptr, const int32_t* side_cols,
-                                       const float* side_w, int64_t side_count, const void* events, bp_etype etype,
-                                       float* out, int32_t cluster, void* workspace, size_t workspace_bytes,
-                                       bp_stream_t stream) {
+size_t bp_csr_plan_fix_interleave_bytes(const bp_csr_plan* plan) {
+  if (!plan) return 0;
+  return (size_t)(plan->entries / 8) * 48;
+}
+
+bp_status bp_csr_plan_fix_interleave(const bp_csr_plan* plan, void* fx, size_t fx_bytes, bp_stream_t stream) {
+  clear_error();
+  BP_REQUIRE(plan != nullptr && plan->mem != nullptr && plan->kind == 2, BP_EINVAL,
+             "csr_plan_fix_interleave: needs a fixed-weight plan");
+  const size_t need = bp_csr_plan_fix_interleave_bytes(plan);
+  BP_REQUIRE(fx != nullptr && fx_bytes >= need && (reinterpret_cast<uintptr_t>(fx) & 15u) == 0, BP_EINVAL,
+             "csr_plan_fix_interleave: %zu bytes at %p, need %zu on a 16-byte boundary", fx_bytes, fx, need);
+  PlanView v = plan_view(plan);
+  const uint64_t nchunks = plan->entries / 8;
+  if (nchunks == 0) return BP_OK;
+  const uint64_t g = std::min<uint64_t>((nchunks + 255) / 256, (uint64_t)device_sm_count() * 32);
+  fix_interleave_kernel<<<(unsigned)g, 256, 0, as_cuda(stream)>>>(reinterpret_cast<const uint4*>(v.idx),
+                                                                 reinterpret_cast<const uint4*>(v.w),
+                                                                 static_cast<uint4*>(fx), nchunks);
+  return check_launch("fix_interleave_kernel");
+}
+
+bp_status bp_event_csrmv_planned_fixed(const bp_csr_plan* plan, const void* fx, const int32_t* side_ptr,
+                                       const int32_t* side_cols, const float* side_w, int64_t side_count,
+                                       const void* events, bp_etype etype, float* out, int32_t cluster,
+                                       void* workspace, size_t workspace_bytes, bp_stream_t stream) {
   clear_error();
   BP_REQUIRE(side_count >= 0 && (side_count == 0 || (side_ptr && side_cols && side_w)), BP_EINVAL,
              "event_csrmv_planned_fixed: null side arrays for %lld entries", (long long)side_count);
-  FixSide side{side_ptr, side_cols, side_w, side_count};
+  BP_REQUIRE(fx != nullptr && (reinterpret_cast<uintptr_t>(fx) & 15u) == 0, BP_EINVAL,
+             "event_csrmv_planned_fixed: the interleaved chunks (bp_csr_plan_fix_interleave) are required");
+  FixSide side{side_ptr, side_cols, side_w, side_count, static_cast<const uint4*>(fx)};
   return planned_batch("event_csrmv_planned_fixed", plan, nullptr, events, etype, false, 1, out, cluster, workspace,
                        workspace_bytes, as_cuda(stream), &side);
 }

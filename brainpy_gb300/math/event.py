@@ -109,6 +109,11 @@ class CSRPlan:
     self.side = (ptr, cols.contiguous(), ws.contiguous(), count)
     self.fix_exponent, self.fix_tau = k, tau
     self.kind = "fixed"
+    # the chunks as 48-byte records (indices, integer weights): one read a segment
+    fxb = int(L.bp_csr_plan_fix_interleave_bytes(ctypes.byref(self.c)))
+    self.fx = torch.empty(max(fxb, 16), dtype=torch.uint8, device=dev)
+    _lib.check(L.bp_csr_plan_fix_interleave(ctypes.byref(self.c), _lib.ptr(self.fx), self.fx.numel(), sp),
+               "csr_plan_fix_interleave")
 
   def _workspace(self, stream_ptr, nbytes=None):
     nbytes = self._ws_bytes if nbytes is None else nbytes
@@ -132,9 +137,9 @@ class CSRPlan:
     sp = _lib.raw_stream(self.device)
     if self.side is not None:
       ptr, cols, ws, count = self.side
-      st = self._L.bp_event_csrmv_planned_fixed(self._cref, ptr.data_ptr(), cols.data_ptr(), ws.data_ptr(), count,
-                                                ev.data_ptr(), etype, out.data_ptr(), self.cluster,
-                                                self._workspace(sp).data_ptr(), self._ws_bytes, sp)
+      st = self._L.bp_event_csrmv_planned_fixed(self._cref, self.fx.data_ptr(), ptr.data_ptr(), cols.data_ptr(),
+                                                ws.data_ptr(), count, ev.data_ptr(), etype, out.data_ptr(),
+                                                self.cluster, self._workspace(sp).data_ptr(), self._ws_bytes, sp)
       if st:
         _lib.check(st, "event_csrmv_planned_fixed")
       return out

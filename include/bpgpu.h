@@ -250,10 +250,15 @@ bp_status bp_csr_plan_arrays(const bp_csr_plan* plan, const uint32_t** seg_off, 
 bp_status bp_csr_plan_fix_weights(bp_csr_plan* plan, int32_t k, float tau, int32_t* side_rows, int32_t* side_cols,
                                   float* side_w, int64_t side_cap, uint64_t* side_count, int32_t convert,
                                   bp_stream_t stream);
-bp_status bp_event_csrmv_planned_fixed(const bp_csr_plan* plan, const int32_t* side_ptr, const int32_t* side_cols,
-                                       const float* side_w, int64_t side_count, const void* events, bp_etype etype,
-                                       float* out, int32_t cluster, void* workspace, size_t workspace_bytes,
-                                       bp_stream_t stream);
+/* The fixed-weight call reads each chunk as one 48-byte record (its 8 indices, then its 8 integer
+ * weights), so a segment is one contiguous read: bp_csr_plan_fix_interleave writes them into fx
+ * (bp_csr_plan_fix_interleave_bytes(plan) bytes on a 16-byte boundary, kept beside the plan). */
+size_t bp_csr_plan_fix_interleave_bytes(const bp_csr_plan* plan);
+bp_status bp_csr_plan_fix_interleave(const bp_csr_plan* plan, void* fx, size_t fx_bytes, bp_stream_t stream);
+bp_status bp_event_csrmv_planned_fixed(const bp_csr_plan* plan, const void* fx, const int32_t* side_ptr,
+                                       const int32_t* side_cols, const float* side_w, int64_t side_count,
+                                       const void* events, bp_etype etype, float* out, int32_t cluster,
+                                       void* workspace, size_t workspace_bytes, bp_stream_t stream);
 
 /* event.csrmv, transpose=1, on a plan: out (n) = sum of the active rows.  `w_homo` is the
  * homogeneous weight (device pointer to one float) for homogeneous plans and is ignored for

@@ -100,13 +100,15 @@ class CSRPlan:
     ws = torch.empty(max(count, 1), dtype=torch.float32, device=dev)
     _lib.check(L.bp_csr_plan_fix_weights(ctypes.byref(self.c), k, tau, _lib.ptr(rows), _lib.ptr(cols), _lib.ptr(ws),
                                          count, _lib.ptr(cnt), 1, sp), "csr_plan_fix_weights")
-    m = self.shape[0]
     order = torch.argsort(rows[:count].to(torch.int64), stable=True)
     rows, cols, ws = rows[:count][order], cols[:count][order], ws[:count][order]
-    ptr = torch.zeros(m + 1, dtype=torch.int32, device=dev)
+    # the rows that hold side entries, each with its range of entries
+    urows, per_row = torch.unique_consecutive(rows, return_counts=True)
+    ptr = torch.zeros(urows.numel() + 1, dtype=torch.int32, device=dev)
     if count:
-      ptr[1:] = torch.cumsum(torch.bincount(rows.to(torch.int64), minlength=m), 0).to(torch.int32)
-    self.side = (ptr, cols.contiguous(), ws.contiguous(), count)
+      ptr[1:] = torch.cumsum(per_row, 0).to(torch.int32)
+    self.side = (urows.to(torch.int32).contiguous(), ptr, cols.contiguous(), ws.contiguous(), int(urows.numel()))
+    self.side_entries = count
     self.fix_exponent, self.fix_tau = k, tau
     self.kind = "fixed"
     # the chunks as 48-byte records (indices, integer weights): one read a segment
@@ -136,10 +138,11 @@ class CSRPlan:
       w = (data if data is not None else self._one).data_ptr()
     sp = _lib.raw_stream(self.device)
     if self.side is not None:
-      ptr, cols, ws, count = self.side
-      st = self._L.bp_event_csrmv_planned_fixed(self._cref, self.fx.data_ptr(), ptr.data_ptr(), cols.data_ptr(),
-                                                ws.data_ptr(), count, ev.data_ptr(), etype, out.data_ptr(),
-                                                self.cluster, self._workspace(sp).data_ptr(), self._ws_bytes, sp)
+      urows, ptr, cols, ws, nrows = self.side
+      st = self._L.bp_event_csrmv_planned_fixed(self._cref, self.fx.data_ptr(), urows.data_ptr(), ptr.data_ptr(),
+                                                cols.data_ptr(), ws.data_ptr(), nrows, ev.data_ptr(), etype,
+                                                out.data_ptr(), self.cluster, self._workspace(sp).data_ptr(),
+                                                self._ws_bytes, sp)
       if st:
         _lib.check(st, "event_csrmv_planned_fixed")
       return out

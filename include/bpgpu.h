@@ -243,7 +243,8 @@ bp_status bp_csr_plan_arrays(const bp_csr_plan* plan, const uint32_t** seg_off, 
  * times 2^k reaches 2^31) and lists the nonzero weights with |w| < tau as (row, column, w) in
  * side_rows / side_cols / side_w (up to side_cap of them; *side_count, a device word, receives the
  * full count).  With convert = 0 it only counts them.  The caller sorts the listed entries by row
- * into side_ptr[m + 1] / side_cols / side_w for bp_event_csrmv_planned_fixed, which adds the fixed-
+ * and passes the rows that hold any (side_rows[0 .. side_nrows)) with each one's entries at
+ * [side_ptr[i], side_ptr[i + 1]) of side_cols / side_w to bp_event_csrmv_planned_fixed, which adds the fixed-
  * point weights with exact integer shared-memory adds (out = (float)sum * 2^-k) and then the listed
  * weights with float atomics.  With tau = 2^-(k+1) / 5e-6 every fixed-point term is within 5e-6
  * of its weight, relative, so a sum stays within 1e-5 of the exact sum of its terms' magnitudes. */
@@ -255,10 +256,11 @@ bp_status bp_csr_plan_fix_weights(bp_csr_plan* plan, int32_t k, float tau, int32
  * (bp_csr_plan_fix_interleave_bytes(plan) bytes on a 16-byte boundary, kept beside the plan). */
 size_t bp_csr_plan_fix_interleave_bytes(const bp_csr_plan* plan);
 bp_status bp_csr_plan_fix_interleave(const bp_csr_plan* plan, void* fx, size_t fx_bytes, bp_stream_t stream);
-bp_status bp_event_csrmv_planned_fixed(const bp_csr_plan* plan, const void* fx, const int32_t* side_ptr,
-                                       const int32_t* side_cols, const float* side_w, int64_t side_count,
-                                       const void* events, bp_etype etype, float* out, int32_t cluster,
-                                       void* workspace, size_t workspace_bytes, bp_stream_t stream);
+bp_status bp_event_csrmv_planned_fixed(const bp_csr_plan* plan, const void* fx, const int32_t* side_rows,
+                                       const int32_t* side_ptr, const int32_t* side_cols, const float* side_w,
+                                       int64_t side_nrows, const void* events, bp_etype etype, float* out,
+                                       int32_t cluster, void* workspace, size_t workspace_bytes,
+                                       bp_stream_t stream);
 
 /* event.csrmv, transpose=1, on a plan: out (n) = sum of the active rows.  `w_homo` is the
  * homogeneous weight (device pointer to one float) for homogeneous plans and is ignored for

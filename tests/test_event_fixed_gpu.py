@@ -48,7 +48,7 @@ def test_fixed_plan_against_oracle(ev, orc, law):
   w_h = w.astype(np.float32)
   plan = ev.CSRPlan(ind, ptr, (m, n), data=torch.as_tensor(w_h, device="cuda"), kind="fixed")
   assert plan.kind == "fixed" and plan.c.kind == 2
-  side = plan.side[3]
+  side = plan.side_entries
   if law == "positive":
     assert side == 0
   if law in ("normal_0_1", "wide"):

@@ -61,10 +61,10 @@ SIGNATURES = {
     "bp_csr_plan_count_tile": (_c_i32, [_c_i64]),
     "bp_csr_plan_fix_weights": (_c_i32, [_c_ptr, _c_i32, _c_f32, _c_ptr, _c_ptr, _c_ptr, _c_i64, _c_ptr, _c_i32,
                                          _c_ptr]),
-    "bp_csr_plan_fix_interleave_bytes": (_c_size, [_c_ptr]),
-    "bp_csr_plan_fix_interleave": (_c_i32, [_c_ptr, _c_ptr, _c_size, _c_ptr]),
-    "bp_event_csrmv_planned_fixed": (_c_i32, [_c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i64, _c_ptr,
-                                              _c_i32, _c_ptr, _c_i32, _c_ptr, _c_size, _c_ptr]),
+    "bp_csr_plan_fix_interleave_bytes": (_c_size, [_c_ptr, _c_i32]),
+    "bp_csr_plan_fix_interleave": (_c_i32, [_c_ptr, _c_i32, _c_ptr, _c_size, _c_ptr, _c_ptr]),
+    "bp_event_csrmv_planned_fixed": (_c_i32, [_c_ptr, _c_ptr, _c_i32, _c_ptr, _c_ptr, _c_ptr, _c_ptr, _c_i64,
+                                              _c_ptr, _c_i32, _c_ptr, _c_i32, _c_ptr, _c_size, _c_ptr]),
     "bp_csr_plan_variants": (_c_i32, [_c_ptr, _c_i32]),
     "bp_csr_plan_bytes": (_c_size, [_c_i64, _c_i64, _c_i64, _c_i32, _c_i32]),
     "bp_csr_plan_build": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_i32, _c_ptr,

@@ -190,14 +190,20 @@ __global__ void __launch_bounds__(256) compact_blocked_kernel(const void* __rest
 //   kWRow   heterogeneous weights, dense vector x: float32 sum of w_ij * x_i
 //   kFix    heterogeneous weights held as int32 fixed point (w * 2^k, a fixed-weight plan),
 //           events: exact integer sums, out = (float)sum * 2^-k
-enum { kCount = 0, kWeight = 1, kRowVal = 2, kWRow = 3, kFix = 4 };
+//   kFix24  kFix with the integer weights stored in 24 bits (40-byte chunk records)
+enum { kCount = 0, kWeight = 1, kRowVal = 2, kWRow = 3, kFix = 4, kFix24 = 5 };
+
+__host__ __device__ constexpr bool fixed_mode(int mode) { return mode == kFix || mode == kFix24; }
+__host__ __device__ constexpr bool weighted_mode(int mode) {
+  return mode == kWeight || mode == kWRow || fixed_mode(mode);
+}
 
 // Threads of a tiled CTA: 1024 (64 registers a thread), except the per-synapse-weight modes
 // with two chunk rounds, whose double-buffered 48-byte chunks need more than 64 registers:
 // 768 threads (80 registers) there.
 template <int MODE, int RND>
 constexpr int tiled_threads() {
-  return ((MODE == kWeight || MODE == kWRow || MODE == kFix) && RND >= 2) ? 768 : kTiledThreads;
+  return (weighted_mode(MODE) && RND >= 2) ? 768 : kTiledThreads;
 }
 
 // Shared-memory reductions issued under a predicate (no branch): entries with index >= lim
@@ -211,6 +217,17 @@ __device__ __forceinline__ void red_if(uint32_t x, uint32_t lim, uint32_t addr, 
                "r"(lim), "r"(addr), "f"(v));
 }
 
+// Integer weight j (0..7) of a 40-byte chunk record: the low 16 bits from lo (two a word), the
+// high byte from hi (four a word), sign-extended from bit 23 by the byte permute.
+template <int J>
+__device__ __forceinline__ uint32_t fix24_weight(const uint32_t lo[4], const uint32_t hi[2]) {
+  constexpr uint32_t b0 = 2u * (J & 1), b2 = 4u + (J & 3);
+  constexpr uint32_t sel = b0 | ((b0 + 1u) << 4) | (b2 << 8) | ((8u | b2) << 12);  // 8: replicate the sign
+  uint32_t q;
+  asm("prmt.b32 %0, %1, %2, %3;" : "=r"(q) : "r"(lo[J >> 1]), "r"(hi[J >> 2]), "n"(sel));
+  return q;
+}
+
 // Adds the 8 entries of one chunk (tile-local indices) into the accumulator at shared-memory
 // address acc_s.
 template <int MODE>
@@ -218,6 +235,17 @@ __device__ __forceinline__ void accumulate8(uint32_t acc_s, uint4 v, float4 w0, 
   const uint32_t x[8] = {v.x & 0xFFFFu, v.x >> 16, v.y & 0xFFFFu, v.y >> 16,
                          v.z & 0xFFFFu, v.z >> 16, v.w & 0xFFFFu, v.w >> 16};
   const float ww[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+  if (MODE == kFix24) {  // w0: the 16-bit halves, w1.x / w1.y: the high bytes
+    const uint32_t lo[4] = {__float_as_uint(w0.x), __float_as_uint(w0.y), __float_as_uint(w0.z),
+                            __float_as_uint(w0.w)};
+    const uint32_t hi[2] = {__float_as_uint(w1.x), __float_as_uint(w1.y)};
+    const uint32_t qq[8] = {fix24_weight<0>(lo, hi), fix24_weight<1>(lo, hi), fix24_weight<2>(lo, hi),
+                            fix24_weight<3>(lo, hi), fix24_weight<4>(lo, hi), fix24_weight<5>(lo, hi),
+                            fix24_weight<6>(lo, hi), fix24_weight<7>(lo, hi)};
+#pragma unroll
+    for (int q = 0; q < 8; ++q) asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(acc_s + 4u * x[q]), "r"(qq[q]));
+    return;
+  }
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     const uint32_t ad = acc_s + 4u * x[q];
@@ -235,6 +263,20 @@ __device__ __forceinline__ void accumulate8(uint32_t acc_s, uint4 v, float4 w0, 
 }
 
 __device__ __forceinline__ uint4 ld_stream_u4(const uint16_t* p) { return __ldcs(reinterpret_cast<const uint4*>(p)); }
+
+// 40-byte chunk records of a fixed-weight plan whose integer weights fit in 24 bits: chunk c at
+// byte 40c holds its 8 tile-local indices (16 bytes), the low 16 bits of its 8 weights (16 bytes)
+// and their high bytes (8 bytes).  An even chunk starts on a 16-byte boundary and stores them in
+// that order; an odd chunk starts 8 bytes past one and stores the high bytes first.  Either way
+// the indices and the low halves are 16-byte loads and the high bytes an 8-byte load.
+__device__ __forceinline__ void fix24_load(const uint4* fx, uint64_t c, uint4& idx, float4& lo, float4& hi) {
+  const unsigned char* rec = reinterpret_cast<const unsigned char*>(fx) + 40ull * c;
+  const uint32_t odd = (uint32_t)c & 1u;
+  idx = __ldcs(reinterpret_cast<const uint4*>(rec + 8u * odd));
+  lo = __ldcs(reinterpret_cast<const float4*>(rec + 16u + 8u * odd));
+  const float2 h = __ldcs(reinterpret_cast<const float2*>(rec + 32u - 32u * odd));
+  hi = make_float4(h.x, h.y, 0.0f, 0.0f);
+}
 __device__ __forceinline__ float4 ld_stream_f4(const float* p) { return __ldcs(reinterpret_cast<const float4*>(p)); }
 __device__ __forceinline__ void prefetch_l1(const void* p) {
   asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
@@ -248,8 +290,9 @@ struct TiledArgs {
   const int32_t* counts;
   const float* w_homo;
   const float* row_val;  // dense vector for kRowVal / kWRow
-  const uint32_t* meta;  // plan meta ([2]: the fixed-point exponent of kFix)
-  const uint4* fx;       // kFix: chunk c's 8 indices and 8 integer weights at fx[3c .. 3c + 2]
+  const uint32_t* meta;  // plan meta ([2]: the fixed-point exponent of kFix / kFix24)
+  const uint4* fx;       // kFix: chunk c's 8 indices and 8 integer weights at fx[3c .. 3c + 2];
+                         // kFix24: chunk c's 40-byte record at byte 40c (fix24_record)
   float* out;
   int64_t m, n;  // a batch of vectors: row_val rows of m, out rows of n
   int32_t tile_w, n_tiles, nb, acc_words;
@@ -268,7 +311,7 @@ struct TiledArgs {
 // segment is longer than RND * G chunks also prefetches its next chunk into L1 with the unit.
 template <int MODE, int G, int RND, bool PF, bool BATCH>
 __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_kernel(const TiledArgs a) {
-  constexpr bool HAS_W = (MODE == kWeight || MODE == kWRow || MODE == kFix);
+  constexpr bool HAS_W = weighted_mode(MODE);
   constexpr bool HAS_X = (MODE == kRowVal || MODE == kWRow);
   constexpr unsigned FULL = 0xffffffffu;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -406,12 +449,20 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
             U.vv[u][r] = in ? __ldcs(fp) : lane_pads;
             U.w0[u][r] = in ? __ldcs(reinterpret_cast<const float4*>(fp + 1)) : z;
             U.w1[u][r] = in ? __ldcs(reinterpret_cast<const float4*>(fp + 2)) : z;
+          } else if (MODE == kFix24) {
+            const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (in) fix24_load(a.fx, U.st[u] + c, U.vv[u][r], U.w0[u][r], U.w1[u][r]);
+            else {
+              U.vv[u][r] = lane_pads;
+              U.w0[u][r] = z;
+              U.w1[u][r] = z;
+            }
           } else if (MODE == kCount) {
             U.vv[u][r] = in ? ld_stream_u4(a.idx + e) : lane_pads;
           } else {
             U.vv[u][r] = ld_stream_u4(a.idx + e);
           }
-          if (HAS_W && MODE != kFix) {
+          if (HAS_W && !fixed_mode(MODE)) {
             U.w0[u][r] = ld_stream_f4(a.w + e);
             U.w1[u][r] = ld_stream_f4(a.w + e + 4);
           }
@@ -447,6 +498,8 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
             x = __ldcs(fp);
             y0 = __ldcs(reinterpret_cast<const float4*>(fp + 1));
             y1 = __ldcs(reinterpret_cast<const float4*>(fp + 2));
+          } else if (MODE == kFix24) {
+            fix24_load(a.fx, U.st[u] + c, x, y0, y1);
           } else {
             x = ld_stream_u4(a.idx + e);
             if (HAS_W) {
@@ -495,7 +548,7 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
     for (int r = 0; r < 8; ++r)
       if (r < R) x[r] = *reinterpret_cast<const uint4*>(cluster.map_shared_rank(acc, r) + c);
     float o[4];
-    if (MODE == kCount || MODE == kFix) {
+    if (MODE == kCount || fixed_mode(MODE)) {
       uint4 s = make_uint4(0, 0, 0, 0);
 #pragma unroll
       for (int r = 0; r < 8; ++r) {
@@ -506,7 +559,7 @@ __global__ void __launch_bounds__(tiled_threads<MODE, RND>(), 1) ecsr_t_tiled_ke
           s.w += x[r].w;
         }
       }
-      if (MODE == kFix) {  // two's-complement sums; 2^-k is exact
+      if (fixed_mode(MODE)) {  // two's-complement sums; 2^-k is exact
         const float sc = __int_as_float((127 - (int)__ldg(a.meta + 2)) << 23);
         o[0] = __fmul_rn((float)(int32_t)s.x, sc);
         o[1] = __fmul_rn((float)(int32_t)s.y, sc);
@@ -1094,10 +1147,12 @@ static void tiled_config(double chunks, bool has_w, int32_t variant, int& G, int
 template <int MODE>
 static bp_status launch_tiled(const TiledArgs& a, int R, double chunks, cudaStream_t st) {
   int G, RND, PF;
-  tiled_config(chunks, MODE == kWeight || MODE == kWRow || MODE == kFix, a.variant, G, RND, PF);
+  tiled_config(chunks, weighted_mode(MODE), a.variant, G, RND, PF);
+  // fixed-weight plans serve one vector a call: no batch instantiation
 #define BP_TILED_CASE(g, r)                                                                           \
   if (G == g && RND == r) {                                                                           \
-    if (a.batch > 1) return launch_tiled_g<MODE, g, r, false, true>(a, R, st);                        \
+    if (!fixed_mode(MODE) && a.batch > 1)                                                             \
+      return launch_tiled_g<MODE, g, r, false, !fixed_mode(MODE)>(a, R, st);                          \
     return PF ? launch_tiled_g<MODE, g, r, true>(a, R, st) : launch_tiled_g<MODE, g, r, false>(a, R, st); \
   }
   BP_TILED_CASE(1, 1)
@@ -1431,7 +1486,8 @@ struct FixSide {
   const int32_t* cols;
   const float* w;
   int64_t nrows;
-  const uint4* fx;  // the plan's chunks as 48-byte records (bp_csr_plan_fix_interleave)
+  const uint4* fx;  // the plan's chunks as records (bp_csr_plan_fix_interleave)
+  int32_t record;   // their size: 48 (int32 weights) or 40 (24-bit weights)
 };
 
 // One thread per row with side entries: if the row's event is on, its entries, float atomics
@@ -1513,7 +1569,7 @@ static bp_status planned_batch(const char* who, const bp_csr_plan* plan, const f
   if (dense) return homo ? launch_tiled<kRowVal>(a, cluster, chunks, st) : launch_tiled<kWRow>(a, cluster, chunks, st);
   if (fixed) {
     a.fx = side->fx;
-    s = launch_tiled<kFix>(a, cluster, chunks, st);
+    s = side->record == 40 ? launch_tiled<kFix24>(a, cluster, chunks, st) : launch_tiled<kFix>(a, cluster, chunks, st);
     if (s != BP_OK || side->nrows == 0) return s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -1582,6 +1638,48 @@ __global__ void __launch_bounds__(256) fix_interleave_kernel(const uint4* __rest
     fx[3 * c] = idx[c];
     fx[3 * c + 1] = w[2 * c];
     fx[3 * c + 2] = w[2 * c + 1];
+  }
+}
+
+// chunk c of a plan -> its 40-byte record at byte 40c (the layout fix24_load reads): indices,
+// low 16 bits of the weights, high bytes (the high bytes first in an odd chunk).  One warp per
+// row walks the row's segments, chunks [seg_off[r][0], seg_off[r][T]): the gaps the plan leaves
+// between rows hold no entries and are not written.  Weights outside [-2^23, 2^23) are counted
+// into *unfit (their records would be wrong).
+__global__ void __launch_bounds__(256) fix_interleave24_kernel(const uint32_t* __restrict__ seg_off,
+                                                               const uint4* __restrict__ idx,
+                                                               const int4* __restrict__ w,
+                                                               unsigned char* __restrict__ fx, int64_t m,
+                                                               int n_tiles, unsigned long long* unfit) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < m; r += nwarps) {
+    const uint32_t* so = seg_off + r * (int64_t)(n_tiles + 1);
+    const uint64_t c1 = so[n_tiles];
+    for (uint64_t c = so[0] + lane; c < c1; c += 32) {
+      const int4 a = w[2 * c], b = w[2 * c + 1];
+      const int32_t q[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+      uint32_t lo[4] = {0u, 0u, 0u, 0u}, hi[2] = {0u, 0u};
+      int bad = 0;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        bad += (q[j] < -(1 << 23) || q[j] >= (1 << 23)) ? 1 : 0;
+        const uint32_t u = (uint32_t)q[j];
+        lo[j >> 1] |= (u & 0xFFFFu) << (16 * (j & 1));
+        hi[j >> 2] |= ((u >> 16) & 0xFFu) << (8 * (j & 3));
+      }
+      if (bad) atomicAdd(unfit, (unsigned long long)bad);
+      const uint4 x = idx[c];
+      uint2* rec = reinterpret_cast<uint2*>(fx + 40ull * c);  // 8-byte aligned
+      const uint2 h = make_uint2(hi[0], hi[1]);
+      const int o = (int)(c & 1u);  // odd: the high bytes first
+      if (o) rec[0] = h;
+      rec[o + 0] = make_uint2(x.x, x.y);
+      rec[o + 1] = make_uint2(x.z, x.w);
+      rec[o + 2] = make_uint2(lo[0], lo[1]);
+      rec[o + 3] = make_uint2(lo[2], lo[3]);
+      if (!o) rec[4] = h;
+    }
   }
 }
 
@@ -1715,29 +1813,42 @@ bp_status bp_csr_plan_fix_weights(bp_csr_plan* plan, int32_t k, float tau, int32
   return BP_OK;
 }
 
-size_t bp_csr_plan_fix_interleave_bytes(const bp_csr_plan* plan) {
-  if (!plan) return 0;
-  return (size_t)(plan->entries / 8) * 48;
+size_t bp_csr_plan_fix_interleave_bytes(const bp_csr_plan* plan, int32_t record_bytes) {
+  if (!plan || (record_bytes != 48 && record_bytes != 40)) return 0;
+  return (size_t)(plan->entries / 8) * (size_t)record_bytes;
 }
 
-bp_status bp_csr_plan_fix_interleave(const bp_csr_plan* plan, void* fx, size_t fx_bytes, bp_stream_t stream) {
+bp_status bp_csr_plan_fix_interleave(const bp_csr_plan* plan, int32_t record_bytes, void* fx, size_t fx_bytes,
+                                     uint64_t* unfit, bp_stream_t stream) {
   clear_error();
   BP_REQUIRE(plan != nullptr && plan->mem != nullptr && plan->kind == 2, BP_EINVAL,
              "csr_plan_fix_interleave: needs a fixed-weight plan");
-  const size_t need = bp_csr_plan_fix_interleave_bytes(plan);
+  BP_REQUIRE(record_bytes == 48 || (record_bytes == 40 && unfit != nullptr), BP_EINVAL,
+             "csr_plan_fix_interleave: records of 48 bytes, or of 40 with an unfit counter (got %d%s)", record_bytes,
+             unfit ? "" : ", no counter");
+  const size_t need = bp_csr_plan_fix_interleave_bytes(plan, record_bytes);
   BP_REQUIRE(fx != nullptr && fx_bytes >= need && (reinterpret_cast<uintptr_t>(fx) & 15u) == 0, BP_EINVAL,
              "csr_plan_fix_interleave: %zu bytes at %p, need %zu on a 16-byte boundary", fx_bytes, fx, need);
   PlanView v = plan_view(plan);
   const uint64_t nchunks = plan->entries / 8;
   if (nchunks == 0) return BP_OK;
   const uint64_t g = std::min<uint64_t>((nchunks + 255) / 256, (uint64_t)device_sm_count() * 32);
+  if (record_bytes == 40) {
+    if (plan->m <= 0) return BP_OK;
+    const int64_t gr = std::min<int64_t>((plan->m + 7) / 8, (int64_t)device_sm_count() * 16);
+    fix_interleave24_kernel<<<(unsigned)gr, 256, 0, as_cuda(stream)>>>(
+        v.seg_off, reinterpret_cast<const uint4*>(v.idx), reinterpret_cast<const int4*>(v.w),
+        static_cast<unsigned char*>(fx), plan->m, plan->n_tiles, reinterpret_cast<unsigned long long*>(unfit));
+    return check_launch("fix_interleave24_kernel");
+  }
   fix_interleave_kernel<<<(unsigned)g, 256, 0, as_cuda(stream)>>>(reinterpret_cast<const uint4*>(v.idx),
                                                                  reinterpret_cast<const uint4*>(v.w),
                                                                  static_cast<uint4*>(fx), nchunks);
   return check_launch("fix_interleave_kernel");
 }
 
-bp_status bp_event_csrmv_planned_fixed(const bp_csr_plan* plan, const void* fx, const int32_t* side_rows,
+bp_status bp_event_csrmv_planned_fixed(const bp_csr_plan* plan, const void* fx, int32_t record_bytes,
+                                       const int32_t* side_rows,
                                        const int32_t* side_ptr, const int32_t* side_cols, const float* side_w,
                                        int64_t side_nrows, const void* events, bp_etype etype, float* out,
                                        int32_t cluster, void* workspace, size_t workspace_bytes,
@@ -1747,7 +1858,9 @@ bp_status bp_event_csrmv_planned_fixed(const bp_csr_plan* plan, const void* fx, 
              "event_csrmv_planned_fixed: null side arrays for %lld rows", (long long)side_nrows);
   BP_REQUIRE(fx != nullptr && (reinterpret_cast<uintptr_t>(fx) & 15u) == 0, BP_EINVAL,
              "event_csrmv_planned_fixed: the interleaved chunks (bp_csr_plan_fix_interleave) are required");
-  FixSide side{side_rows, side_ptr, side_cols, side_w, side_nrows, static_cast<const uint4*>(fx)};
+  BP_REQUIRE(record_bytes == 48 || record_bytes == 40, BP_EINVAL,
+             "event_csrmv_planned_fixed: records of 48 or 40 bytes (got %d)", record_bytes);
+  FixSide side{side_rows, side_ptr, side_cols, side_w, side_nrows, static_cast<const uint4*>(fx), record_bytes};
   return planned_batch("event_csrmv_planned_fixed", plan, nullptr, events, etype, false, 1, out, cluster, workspace,
                        workspace_bytes, as_cuda(stream), &side);
 }

@@ -31,7 +31,7 @@ class CSRPlan:
   own device memory; it is a function of the arrays at build time.
   """
 
-  def __init__(self, indices, indptr, shape, data=None, tile_w=None, cluster=4, kind="general"):
+  def __init__(self, indices, indptr, shape, data=None, tile_w=None, cluster=4, kind="general", fix_record=None):
     dev = indices.device
     self.shape = (int(shape[0]), int(shape[1]))
     self.cluster = int(cluster)
@@ -42,6 +42,8 @@ class CSRPlan:
       raise ValueError(f"plan kind must be 'general', 'count' or 'fixed', got {kind!r}")
     if kind == "fixed" and not heter:
       raise ValueError("a fixed-weight plan needs per-synapse weights")
+    if fix_record not in (None, 40, 48):
+      raise ValueError(f"fix_record must be None, 40 or 48, got {fix_record!r}")
     # "count": tiles of up to 65,472 columns with 16-bit counters and per-tile partial counts
     # (event products with a homogeneous weight, one vector a call); "general": tiles whose
     # 32-bit accumulator fits one CTA (every product, batches, weights)
@@ -69,7 +71,7 @@ class CSRPlan:
     self.device = dev
     self.side = None
     if kind == "fixed":
-      self._fix_weights(data, indices, n)
+      self._fix_weights(data, indices, n, fix_record if fix_record is not None else _FIX_RECORD)
     # per-call state kept ready: the C plan struct, a unit weight, and one workspace per stream
     # (calls on one stream are ordered, so they can share it)
     self._L = L
@@ -78,10 +80,12 @@ class CSRPlan:
     self._ws_bytes = L.bp_event_csrmv_planned_workspace_size(self._cref)
     self._ws = {}
 
-  def _fix_weights(self, data, indices, n):
+  def _fix_weights(self, data, indices, n, record=None):
     """Fixed-point weights: k from the largest column sum of |w| (no column's sum times 2^k
     reaches 2^31 - 2^24), tau = 2^-(k+1) / 5e-6; the weights below tau go to the side list,
-    sorted by row."""
+    sorted by row.  The chunks are stored as 40-byte records (24-bit weights) when every
+    max |w| * 2^k < 2^23 - 1 and `record` is not 48, else as 48-byte records (int32 weights);
+    both give the same sums bit for bit."""
     L = _lib.lib()
     dev = self.device
     colsum = torch.zeros(max(n, 1), dtype=torch.float64, device=dev)
@@ -111,11 +115,19 @@ class CSRPlan:
     self.side_entries = count
     self.fix_exponent, self.fix_tau = k, tau
     self.kind = "fixed"
-    # the chunks as 48-byte records (indices, integer weights): one read a segment
-    fxb = int(L.bp_csr_plan_fix_interleave_bytes(ctypes.byref(self.c)))
+    # the chunks as records (indices, integer weights): one read a segment
+    wmax = float(data.abs().max()) if data.numel() else 0.0
+    rec = 40 if record != 48 and wmax * 2.0 ** k < 2.0 ** 23 - 1 else 48
+    if record == 40 and rec != 40:
+      raise ValueError(f"40-byte records need max |w| * 2^k < 2^23 - 1 (max |w| = {wmax}, k = {k})")
+    fxb = int(L.bp_csr_plan_fix_interleave_bytes(ctypes.byref(self.c), rec))
     self.fx = torch.empty(max(fxb, 16), dtype=torch.uint8, device=dev)
-    _lib.check(L.bp_csr_plan_fix_interleave(ctypes.byref(self.c), _lib.ptr(self.fx), self.fx.numel(), sp),
-               "csr_plan_fix_interleave")
+    cnt.zero_()
+    _lib.check(L.bp_csr_plan_fix_interleave(ctypes.byref(self.c), rec, _lib.ptr(self.fx), self.fx.numel(),
+                                            _lib.ptr(cnt), sp), "csr_plan_fix_interleave")
+    if rec == 40 and int(cnt.item()):
+      raise _lib.BPError(f"csr_plan_fix_interleave: {int(cnt.item())} weights outside 24 bits")
+    self.fix_record = rec
 
   def _workspace(self, stream_ptr, nbytes=None):
     nbytes = self._ws_bytes if nbytes is None else nbytes
@@ -139,9 +151,9 @@ class CSRPlan:
     sp = _lib.raw_stream(self.device)
     if self.side is not None:
       urows, ptr, cols, ws, nrows = self.side
-      st = self._L.bp_event_csrmv_planned_fixed(self._cref, self.fx.data_ptr(), urows.data_ptr(), ptr.data_ptr(),
-                                                cols.data_ptr(), ws.data_ptr(), nrows, ev.data_ptr(), etype,
-                                                out.data_ptr(), self.cluster, self._workspace(sp).data_ptr(),
+      st = self._L.bp_event_csrmv_planned_fixed(self._cref, self.fx.data_ptr(), self.fix_record, urows.data_ptr(),
+                                                ptr.data_ptr(), cols.data_ptr(), ws.data_ptr(), nrows, ev.data_ptr(),
+                                                etype, out.data_ptr(), self.cluster, self._workspace(sp).data_ptr(),
                                                 self._ws_bytes, sp)
       if st:
         _lib.check(st, "event_csrmv_planned_fixed")
@@ -306,6 +318,9 @@ _SPLIT_MIN_N = int(os.environ.get("BPGPU_SPLIT_MIN_N", 1 << 62))
 # per-synapse weights take the fixed-point plan whenever the plan path is taken (N = 1e6,
 # fan-out 1000, 2 %: 51.4 against 61.1 us a call); BPGPU_FIXED_MIN_N raises the threshold
 _FIXED_MIN_N = int(os.environ.get("BPGPU_FIXED_MIN_N", 0))
+# chunk records of fixed-weight plans: 0 picks 40 bytes (24-bit weights) where the weights fit,
+# 48 (BPGPU_FIX_RECORD=48) keeps int32 weights
+_FIX_RECORD = int(os.environ.get("BPGPU_FIX_RECORD", 0)) or None
 
 
 def _ident(t):

@@ -251,12 +251,19 @@ bp_status bp_csr_plan_arrays(const bp_csr_plan* plan, const uint32_t** seg_off, 
 bp_status bp_csr_plan_fix_weights(bp_csr_plan* plan, int32_t k, float tau, int32_t* side_rows, int32_t* side_cols,
                                   float* side_w, int64_t side_cap, uint64_t* side_count, int32_t convert,
                                   bp_stream_t stream);
-/* The fixed-weight call reads each chunk as one 48-byte record (its 8 indices, then its 8 integer
- * weights), so a segment is one contiguous read: bp_csr_plan_fix_interleave writes them into fx
- * (bp_csr_plan_fix_interleave_bytes(plan) bytes on a 16-byte boundary, kept beside the plan). */
-size_t bp_csr_plan_fix_interleave_bytes(const bp_csr_plan* plan);
-bp_status bp_csr_plan_fix_interleave(const bp_csr_plan* plan, void* fx, size_t fx_bytes, bp_stream_t stream);
-bp_status bp_event_csrmv_planned_fixed(const bp_csr_plan* plan, const void* fx, const int32_t* side_rows,
+/* The fixed-weight call reads each chunk as one record, so a segment is one contiguous read:
+ * bp_csr_plan_fix_interleave writes them into fx (bp_csr_plan_fix_interleave_bytes(plan,
+ * record_bytes) bytes on a 16-byte boundary, kept beside the plan).  record_bytes = 48: the 8
+ * indices, then the 8 int32 weights.  record_bytes = 40: the 8 indices, the low 16 bits of the 8
+ * weights and their high bytes, for weights in [-2^23, 2^23) (when max |w| * 2^k < 2^23 - 1);
+ * the weights outside that range are added to *unfit (a device word, required), and the records
+ * are usable only while it stays 0.  Both forms give the same results bit for bit;
+ * bp_event_csrmv_planned_fixed takes the record size the chunks were written with. */
+size_t bp_csr_plan_fix_interleave_bytes(const bp_csr_plan* plan, int32_t record_bytes);
+bp_status bp_csr_plan_fix_interleave(const bp_csr_plan* plan, int32_t record_bytes, void* fx, size_t fx_bytes,
+                                     uint64_t* unfit, bp_stream_t stream);
+bp_status bp_event_csrmv_planned_fixed(const bp_csr_plan* plan, const void* fx, int32_t record_bytes,
+                                       const int32_t* side_rows,
                                        const int32_t* side_ptr, const int32_t* side_cols, const float* side_w,
                                        int64_t side_nrows, const void* events, bp_etype etype, float* out,
                                        int32_t cluster, void* workspace, size_t workspace_bytes,

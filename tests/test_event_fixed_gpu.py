@@ -3,7 +3,7 @@ transpose with per-synapse weights held as int32 fixed point (exact integer shar
 out = sum * 2^-k), the weights too small for the fixed point added in float from a side list.
 Against the oracle within the 1e-5 bar scaled by the sum of the terms' magnitudes, for weight
 laws with and without side entries, both event types and rules, both index types, and at the
-benchmarked size."""
+benchmarked size; the 40-byte chunk records (24-bit weights) against the 48-byte ones (int32)."""
 import numpy as np
 import pytest
 import torch
@@ -72,6 +72,7 @@ def test_fixed_plan_full_size(ev, orc):
   ind, ptr = fixed_prob_csr(n, n, k, seed=0)
   w = normal_weights(ind.numel(), 0.5, 0.1, seed=1)
   plan = ev.CSRPlan(ind, ptr, (n, n), data=w, kind="fixed")
+  assert plan.fix_record == 40  # N(0.5, 0.1) at fan-in ~1000: the weights fit 24 bits
   events = bernoulli_events(n, 0.02, seed=2)
   y = plan.csrmv(events).cpu().numpy()
   r = orc.event_csrmv(w.cpu().numpy(), ind.cpu().numpy(), ptr.cpu().numpy(), events.cpu().numpy(), (n, n), True)
@@ -110,3 +111,92 @@ def test_fixed_route_through_public_call(ev, orc, monkeypatch):
   finally:
     ev._ROUTES.pop(key, None)
     ev.release_plans()
+
+
+def _plan_chunks(plan):
+  """The plan's own chunks: a mask of those that belong to a segment (the plan leaves unused
+  gaps between rows; row r's segments are chunks [seg_off[r][0], seg_off[r][T])), and every
+  chunk's 8 indices and 8 integer weights (the plan's weight array after the conversion)."""
+  import ctypes
+  from brainpy_gb300 import _lib
+  so_p, idx_p, w_p = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+  _lib.check(_lib.lib().bp_csr_plan_arrays(ctypes.byref(plan.c), ctypes.byref(so_p), ctypes.byref(idx_p),
+                                           ctypes.byref(w_p)), "csr_plan_arrays")
+  m, t = plan.shape[0], int(plan.c.n_tiles)
+  nch = int(plan.c.entries) // 8
+  mem = plan.mem.cpu().numpy()
+  base = plan.mem.data_ptr()
+
+  def arr(p, nbytes, dtype):
+    off = p.value - base
+    return mem[off:off + nbytes].view(dtype)
+
+  so = arr(so_p, 4 * m * (t + 1), np.uint32).reshape(m, t + 1).astype(np.int64)
+  d = np.zeros(nch + 1, np.int64)
+  np.add.at(d, so[:, 0], 1)
+  np.add.at(d, so[:, t], -1)
+  seg = np.cumsum(d)[:nch] > 0
+  return seg, arr(idx_p, 16 * nch, np.uint16).reshape(nch, 8), arr(w_p, 32 * nch, np.int32).reshape(nch, 8)
+
+
+def _decode48(fx, nchunks):
+  """(indices, integer weights) of every chunk from 48-byte records."""
+  rec = fx[:48 * nchunks].reshape(nchunks, 48)
+  return rec[:, :16].copy().view(np.uint16), rec[:, 16:].copy().view(np.int32)
+
+
+def _decode40(fx, nchunks):
+  """(indices, integer weights) of every chunk from 40-byte records: an even chunk holds its
+  indices, the low 16 bits of its weights and their high bytes; an odd one the high bytes first."""
+  rec = fx[:40 * nchunks].reshape(nchunks, 40)
+  odd = (np.arange(nchunks) & 1).astype(bool)[:, None]
+  idx = np.where(odd, rec[:, 8:24], rec[:, 0:16]).copy().view(np.uint16)
+  lo = np.where(odd, rec[:, 24:40], rec[:, 16:32]).copy().view(np.uint16).astype(np.int64)
+  hi = np.where(odd, rec[:, 0:8], rec[:, 32:40]).copy().view(np.int8).astype(np.int64)
+  return idx, (hi * 65536 + lo).astype(np.int32)
+
+
+@pytest.mark.parametrize("law", ["normal_0.5_0.1", "positive", "normal_0_1"])
+def test_fixed_records_40_and_48(ev, orc, law):
+  """At fan-in ~1000, N(0.5, 0.1) and U[0.5, 1] weights fit 24 bits and take 40-byte records by
+  default; each plan's records (40 or 48 bytes) hold that plan's indices and integer weights, and
+  the two forms give the same results (bit for bit without side entries).  N(0, 1) weights reach more than
+  256 times a column's mean: 48-byte records, and 40 is refused."""
+  from brainpy_gb300.connect import fixed_prob_csr
+  m = n = 20000
+  ind, ptr = fixed_prob_csr(m, n, 1000, seed=11)
+  ind_h, ptr_h = ind.cpu().numpy(), ptr.cpu().numpy()
+  rng = np.random.default_rng(12)
+  nnz = ind_h.size
+  if law == "normal_0.5_0.1":
+    w_h = rng.normal(0.5, 0.1, nnz).astype(np.float32)
+  elif law == "positive":
+    w_h = rng.uniform(0.5, 1.0, nnz).astype(np.float32)
+  else:
+    w_h = rng.normal(0.0, 1.0, nnz).astype(np.float32)
+  w = torch.as_tensor(w_h, device="cuda")
+  plan = ev.CSRPlan(ind, ptr, (m, n), data=w, kind="fixed")
+  plan48 = ev.CSRPlan(ind, ptr, (m, n), data=w, kind="fixed", fix_record=48)
+  assert plan48.fix_record == 48
+  if law == "normal_0_1":
+    assert plan.fix_record == 48
+    with pytest.raises(ValueError):
+      ev.CSRPlan(ind, ptr, (m, n), data=w, kind="fixed", fix_record=40)
+    return
+  assert plan.fix_record == 40
+  # each plan's records hold its own chunks (two builds may order a segment's entries apart)
+  for p, decode in ((plan, _decode40), (plan48, _decode48)):
+    seg, idx, q = _plan_chunks(p)
+    assert seg.sum() * 8 >= nnz
+    ridx, rq = decode(p.fx.cpu().numpy(), idx.shape[0])
+    assert np.array_equal(ridx[seg], idx[seg]) and np.array_equal(rq[seg], q[seg])
+  if law == "positive":
+    assert plan.side_entries == 0
+  for rate in (0.0, 0.02, 0.3, 1.0):
+    e = torch.as_tensor(rng.random(m) < rate, device="cuda")
+    y40, y48 = plan.csrmv(e), plan48.csrmv(e)
+    if law == "positive":
+      assert torch.equal(y40, y48)
+    r = orc.event_csrmv(w_h, ind_h, ptr_h, e.cpu().numpy(), (m, n), True)
+    assert scaled_err(y40.cpu().numpy(), r["out64"], r["abs64"]) < TOL
+    assert scaled_err(y48.cpu().numpy(), r["out64"], r["abs64"]) < TOL

@@ -326,6 +326,19 @@ def main():
   torch.cuda.synchronize()
   cold_ms = sum(a_.elapsed_time(b_) for a_, b_ in cold) / len(cold)
 
+  # The same `steps` public calls issued eagerly, back to back (no graph: the Python call, the
+  # plan-cache lookup and the two launches are in every call), as the median of 20 rounds.
+  eager = []
+  for _ in range(20):
+    a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a_.record()
+    for i in range(args.steps):
+      step(i)
+    b_.record()
+    eager.append((a_, b_))
+  torch.cuda.synchronize()
+  eager_ms = sorted(a_.elapsed_time(b_) / args.steps for a_, b_ in eager)[len(eager) // 2]
+
   # e2e through the public API: each step copies its spike vector from pinned host memory,
   # calls event.csrmv on it and copies the result back into pinned host memory.  The steps are
   # captured in one CUDA graph (the copies become graph memcpy nodes), so every byte of every
@@ -410,6 +423,7 @@ def main():
           "config": headline_config(args, ws),
           "roofline": roof, "e2e": e2e, "gpu_launches": None, "clocks": clk,
           "cold_l2_ms_per_call": cold_ms, "sustained": sustained,
+          "eager_ms_per_call": eager_ms,
           "wall_s_timed_loop": t_wall}
   line["gpu_launches"] = args.steps * launches_per_step(args)
   if rank == 0 and ws == 1 and not args.no_cpu_baseline:

@@ -199,8 +199,8 @@ __host__ __device__ constexpr bool weighted_mode(int mode) {
 }
 
 // Threads of a tiled CTA: 1024 (64 registers a thread), except the per-synapse-weight modes
-// with two chunk rounds, whose double-buffered 48-byte chunks need more than 64 registers:
-// 768 threads (80 registers) there.
+// with two chunk rounds, whose double-buffered 40- or 48-byte chunks need more than 64
+// registers: 768 threads (80 registers) there.
 template <int MODE, int RND>
 constexpr int tiled_threads() {
   return (weighted_mode(MODE) && RND >= 2) ? 768 : kTiledThreads;
@@ -1115,8 +1115,11 @@ static void tiled_config(double chunks, bool has_w, int32_t variant, int& G, int
   // lengths spread as a multinomial), back-to-back calls:
   //   counts (homogeneous weight): G=2, RND=2 30.7 us at 2 % events, 100.0 at 10 %; G=4, RND=1
   //     34.6 / 127.9; flat distribution 33.0 and G=8 38.0 at 2 %;
-  //   per-synapse weights (48 bytes a chunk): G=4, RND=1 58.9 / 237.7; G=8, RND=1 61.5 / 252.8;
-  //     G=2, RND=1 64.4 / 269.6; G=2, RND=2 (768 threads) 65.8 / 260.7.
+  //   per-synapse float weights (index and weight arrays, 48 bytes a chunk): G=4, RND=1
+  //     58.9 / 237.7; G=8, RND=1 61.5 / 252.8; G=2, RND=1 64.4 / 269.6; G=2, RND=2 (768
+  //     threads) 65.8 / 260.7;
+  //   fixed-weight plans (48-byte records) at 2 %: G=4, RND=1 46.7; G=2, RND=2 49.5; G=8,
+  //     RND=1 51.7; G=8, RND=2 60.6; G=2, RND=1 61.3; G=1 71.3.
   if (chunks <= 1.25) { G = 1; RND = 1; }
   else if (chunks <= 2.5) { G = 2; RND = 1; }
   else if (chunks <= 5.0) { G = has_w ? 4 : 2; RND = has_w ? 1 : 2; }

@@ -478,7 +478,7 @@ def north_star_forms(args):
       "config": r["config"]["workload"] + f", {r['steps']} steps timed", "steps_per_s": r["value"],
       "ms_per_step": r["ms_per_step"], "connections_generated_per_s": r["connections_generated_per_s"],
       "synaptic_events_per_s": r["synaptic_events_per_s"], "firing_rate_hz": r["firing_rate_hz"],
-      "push_form": r["push_form"], "clocks": r["clocks"]}
+      "push_form": r["push_form"], "stored_form": r["stored_form"], "clocks": r["clocks"]}
   torch.cuda.empty_cache()
   out["large_network"] = bench_large_network()
   torch.cuda.empty_cache()
@@ -725,13 +725,69 @@ def bench_jitconn_net(args):
                "firing_rate_hz": p_spk / n / (steps * 1e-4), "synaptic_events_per_s": p_spk * 1000 / t_push,
                "barrier_waits_ran_out": bool(push.grid_error()),
                "form": "outdim_parallel=False (atomic=True), whole-GPU persistent runner, one launch"}
+  del push
+  torch.cuda.empty_cache()
+  stored_form = bench_jitconn_stored(n, ne, p, V0, steps, counts)
   return {"metric": "network-steps/s (4M-neuron jitconn E/I network)", "value": steps / t, "unit": "steps/s",
           "n_gpus": 1, "steps": steps, "warmup": 60, "ms_per_step": t / steps * 1e3, "higher_is_better": True,
           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
           "config": {"workload": "4M neurons 80/20, fan-in 1000 via event_mv_prob_homo (outdim_parallel=True), "
                                  "we=0.6 wi=0.536 (COBA's we, its wi x 80/1000: ~2 % firing a step)"},
           "synaptic_events_per_s": n_spk * 1000 / t, "connections_generated_per_s": 4e9 / (t / steps),
-          "firing_rate_hz": n_spk / n / (steps * 1e-4), "push_form": push_form, "clocks": clk}
+          "firing_rate_hz": n_spk / n / (steps * 1e-4), "push_form": push_form, "stored_form": stored_form,
+          "clocks": clk}
+
+
+def bench_jitconn_stored(n, ne, p, V0, steps, counts):
+  """The same pull-form network with its connectivity generated once and stored
+  (EINetwork.materialize: a presynaptic-row CSR of the same connections), stepped by the
+  event-driven CSR products on the per-operator path replayed from CUDA graphs of 50 steps.
+  The two products are autotuned (EINetwork.tune_ops) on the spikes after 60 steps; the
+  network is then reset and run again from the initial state, and its spike counts are
+  compared with the just-in-time run's (`counts`, 60 + `steps` steps).  A failure is
+  reported in the form instead of ending the bench."""
+  from brainpy_gb300 import dyn
+  try:
+    jit = dyn.EINetwork(n, ne, jitconn=dict(prob=p, seeds=(11, 12, 13, 14)), we=0.6, wi=6.7 * 0.08, V0=V0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    net = jit.materialize()
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t0
+    del jit
+    mc = torch.zeros(steps + 60, dtype=torch.int32, device="cuda")
+    t0 = time.perf_counter()
+    net.run(60, method="ops", graph_steps=50, spike_counts=mc[:60])  # builds the two plans
+    torch.cuda.synchronize()
+    t_warm = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    recs = net.tune_ops()
+    t_tune = time.perf_counter() - t0
+    dev = torch.device("cuda")
+    net.reset_state(torch.as_tensor(V0, device=dev), torch.zeros(n, device=dev), torch.zeros(n, device=dev),
+                    torch.full((n,), -1e7, device=dev), torch.zeros(n, dtype=torch.bool, device=dev))
+    mc.zero_()
+    net.run(60, method="ops", graph_steps=50, spike_counts=mc[:60])
+    clocks = ClockSampler(torch.cuda.current_device())
+    t, _ = _cuda_time(lambda: net.run(steps, method="ops", graph_steps=50, spike_counts=mc[60:]))
+    clk = clocks.stop()
+    nnz = int(net.indices.numel())
+    spk = int(mc[60:].sum())
+    out = {"steps_per_s": steps / t, "ms_per_step": t / steps * 1e3, "synapses_stored": nnz,
+           "index_bytes": nnz * net.indices.element_size(), "generate_s": t_gen,
+           "first_60_steps_s_incl_plan_build": t_warm, "tune_s": t_tune,
+           "tuned_choices": {"excitatory_rows": recs[0]["choice"], "inhibitory_rows": recs[1]["choice"]},
+           "tuned_times_us": {"excitatory_rows": recs[0]["times_us"], "inhibitory_rows": recs[1]["times_us"]},
+           "synaptic_events_per_s_at_mean_out_degree": spk * nnz / n / t,
+           "same_spike_counts_as_jitconn": bool(torch.equal(mc, counts)),
+           "form": "pull connectivity generated once into a presynaptic-row CSR (bp_jitconn_csr), event-driven "
+                   "CSR products, per-operator path from CUDA graphs of 50 steps", "clocks": clk}
+    del net
+    torch.cuda.empty_cache()
+    return out
+  except Exception as e:  # noqa: BLE001 -- reported, not raised
+    torch.cuda.empty_cache()
+    return {"error": f"{type(e).__name__}: {str(e)[:300]}"}
 
 
 def bench_serve(args):

@@ -55,6 +55,8 @@ SIGNATURES = {
     "bp_csr_to_dense": (_c_i32, [_c_ptr, _c_i64, _c_ptr, _c_ptr, _c_i32, _c_i64, _c_i64, _c_i64, _c_ptr, _c_ptr]),
     "bp_jitconn_mv": (_c_i32, [_c_i32, _c_i32, _c_ptr, _c_i64, _c_i64, _c_f32, _c_f32, _c_i32, _c_u32, _c_i32, _c_i32,
                                _c_ptr, _c_ptr]),
+    "bp_jitconn_csr": (_c_i32, [_c_i32, _c_i32, _c_u32, _c_i64, _c_i64, _c_ptr, _c_ptr, _c_i64, _c_ptr, _c_i64, _c_i32,
+                                _c_ptr]),
     "bp_jitconn_dense": (_c_i32, [_c_i32, _c_f32, _c_f32, _c_i32, _c_u32, _c_i64, _c_i64, _c_i32, _c_i32, _c_ptr,
                                   _c_ptr]),
     "bp_csr_plan_default_tile": (_c_i32, [_c_i64, _c_i32]),

@@ -344,6 +344,57 @@ static bp_status launch_mv_vk(const JcArgs& a, int vk, int odp, int variant, cud
   }
 }
 
+// ---------------------------------------------------------------------------
+// The pull connectivity of one homogeneous projection, stored (Taichi GPU algorithm,
+// outdim_parallel=1): for every input column c, the output rows whose lane streams visit c --
+// the presynaptic-row CSR that the event-driven kernels stream, so that a network whose
+// connectivity would be regenerated every step can be run from memory instead.  Stream
+// (row, l) only visits stripe l, columns c with l * step <= c < min(l * step - 1 + step,
+// num_col), so block (l, part) owns one part [lo, hi) of that stripe (at most kJcCsrWidth
+// columns, a 32-bit counter each in shared memory) and walks the lane-l stream of every row
+// up to hi.  PASS 0 counts each owned column's rows into counts[c]; PASS 1 writes
+// row + row_offset at base[c] + the row's rank among the column's rows (a shared-memory
+// cursor: the order inside a column is the order the threads reach it); a position at or past
+// nnz (a base inconsistent with the counts) is skipped.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kJcCsrWidth = 49152;  // 192 KB of counters
+
+template <int PASS, typename IdxT>
+__global__ void __launch_bounds__(1024, 1) jc_csr_kernel(JcArgs a, uint32_t parts, uint32_t width,
+                                                          uint32_t* __restrict__ counts,
+                                                          const int64_t* __restrict__ base, int64_t row_offset,
+                                                          IdxT* __restrict__ indices, int64_t nnz) {
+  extern __shared__ uint32_t cnt[];
+  const uint32_t l = blockIdx.x / parts, part = blockIdx.x % parts;
+  const uint32_t lim = (uint32_t)a.num_col;
+  uint32_t end = a.step * l - 1u + a.step;  // the streams' bound (uint32, as in the pull kernels)
+  if (lim < end) end = lim;
+  const uint32_t lo = a.step * l + part * width;
+  if (lo >= end) return;
+  const uint32_t hi = end - lo < width ? end : lo + width;
+  for (uint32_t j = threadIdx.x; j < hi - lo; j += blockDim.x) cnt[j] = 0u;
+  __syncthreads();
+  for (int64_t row = threadIdx.x; row < a.num_row; row += blockDim.x) {
+    Lfsr88 key = lfsr88_key(a.seed + (uint32_t)(row * 32 + l));
+    uint32_t c = a.step * l - 1u;
+    c += lfsr88_inc(key, a.fm);
+    while (c < hi) {
+      if (c >= lo) {
+        const uint32_t r = atomicAdd(&cnt[c - lo], 1u);
+        if (PASS == 1) {
+          const int64_t at = base[c] + (int64_t)r;
+          if (at >= 0 && at < nnz) indices[at] = (IdxT)(row + row_offset);
+        }
+      }
+      c += lfsr88_inc(key, a.fm);
+    }
+  }
+  if (PASS == 0) {
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < hi - lo; j += blockDim.x) counts[lo + j] = cnt[j];
+  }
+}
+
 static bp_status jc_common_checks(int32_t kind, int64_t num_row, int64_t num_col, int32_t clen, int32_t variant,
                                   const char* who) {
   BP_REQUIRE(kind >= BP_JC_HOMO && kind <= BP_JC_NORMAL, BP_EINVAL, "%s: bad kind %d", who, (int)kind);
@@ -429,6 +480,62 @@ bp_status bp_jitconn_dense(bp_jc_kind kind, float p0, float p1, int32_t clen, ui
     else jc_dense_cpu_kernel<JC_NORMAL><<<g, 256, 0, st>>>(a, odp, dense);
   }
   return check_launch("jitconn_dense kernel");
+}
+
+bp_status bp_jitconn_csr(int32_t pass, int32_t clen, uint32_t seed, int64_t num_row, int64_t num_col,
+                         uint32_t* counts, const int64_t* base, int64_t row_offset, void* indices, int64_t nnz,
+                         bp_itype itype, bp_stream_t stream) {
+  clear_error();
+  cudaStream_t st = as_cuda(stream);
+  bp_status s = jc_common_checks(BP_JC_HOMO, num_row, num_col, clen, BP_JC_TAICHI_GPU, "jitconn_csr");
+  if (s != BP_OK) return s;
+  BP_REQUIRE(pass == 0 || pass == 1, BP_EINVAL, "jitconn_csr: pass must be 0 or 1 (got %d)", (int)pass);
+  BP_REQUIRE(itype == BP_I32 || itype == BP_I64, BP_EDTYPE, "jitconn_csr: bad index type %d", (int)itype);
+  BP_REQUIRE(row_offset >= 0 && (itype == BP_I64 || row_offset + num_row <= (int64_t)INT32_MAX), BP_EINVAL,
+             "jitconn_csr: row ids up to %lld do not fit the index type", (long long)(row_offset + num_row));
+  if (num_row == 0 || num_col == 0) {
+    if (pass == 0 && num_col > 0) {
+      BP_REQUIRE(counts != nullptr, BP_EINVAL, "jitconn_csr: null counts");
+      BP_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(uint32_t) * (size_t)num_col, st));
+    }
+    return BP_OK;
+  }
+  BP_REQUIRE(pass == 1 || counts != nullptr, BP_EINVAL, "jitconn_csr: pass 0 needs counts");
+  BP_REQUIRE(pass == 0 || (base != nullptr && indices != nullptr && nnz >= 0), BP_EINVAL,
+             "jitconn_csr: pass 1 needs base and indices");
+  JcArgs a = make_args(nullptr, nullptr, num_row, num_col, 1.0f, 0.0f, clen, seed);
+  // columns the streams never reach (beyond 32 stripes) keep a count of 0
+  if (pass == 0) BP_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(uint32_t) * (size_t)num_col, st));
+  const uint32_t parts = (a.step + kJcCsrWidth - 1) / kJcCsrWidth;
+  const uint32_t width = (a.step + parts - 1) / parts;
+  const size_t smem = sizeof(uint32_t) * (size_t)width;
+  const dim3 grid(32 * parts);
+  static bool configured[64][4] = {};
+  int dev = 0;
+  BP_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) dev = 0;
+  const int which = pass * 2 + (itype == BP_I64 ? 1 : 0);
+  if (!configured[dev][which]) {
+    const int lim = (int)(sizeof(uint32_t) * kJcCsrWidth);
+    cudaError_t e;
+    if (which == 0) e = cudaFuncSetAttribute(jc_csr_kernel<0, int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    else if (which == 1) e = cudaFuncSetAttribute(jc_csr_kernel<0, int64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    else if (which == 2) e = cudaFuncSetAttribute(jc_csr_kernel<1, int32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    else e = cudaFuncSetAttribute(jc_csr_kernel<1, int64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    BP_CUDA_TRY(e);
+    configured[dev][which] = true;
+  }
+  if (pass == 0) {
+    if (itype == BP_I64) jc_csr_kernel<0, int64_t><<<grid, 1024, smem, st>>>(a, parts, width, counts, nullptr, 0, nullptr, 0);
+    else jc_csr_kernel<0, int32_t><<<grid, 1024, smem, st>>>(a, parts, width, counts, nullptr, 0, nullptr, 0);
+  } else if (itype == BP_I64) {
+    jc_csr_kernel<1, int64_t><<<grid, 1024, smem, st>>>(a, parts, width, nullptr, base, row_offset,
+                                                         static_cast<int64_t*>(indices), nnz);
+  } else {
+    jc_csr_kernel<1, int32_t><<<grid, 1024, smem, st>>>(a, parts, width, nullptr, base, row_offset,
+                                                         static_cast<int32_t*>(indices), nnz);
+  }
+  return check_launch("jc_csr_kernel");
 }
 
 }  // extern "C"

@@ -11,6 +11,8 @@ Two execution forms:
   (bp_net_run); the network must fit one thread-block cluster (n <= 16 x 4096).
 * ``run(..., method="ops")``: one event.csrmv / jitconn call per projection and one
   neuron-update kernel per step (the per-operator path), optionally captured as a CUDA graph.
+A just-in-time network can also be stored (``EINetwork.materialize``): the same connections
+generated once into CSR, stepped by the event-driven CSR products.
 """
 import ctypes
 import math
@@ -152,6 +154,55 @@ class EINetwork:
     indptr = (torch.arange(n + 1, device=dev, dtype=torch.int64) * k_row).to(torch.int32)
     return cls(n, n_exc, indices=indices, indptr=indptr, we=we, wi=wi, params=params, device=dev, V0=V0,
                net_tile=net_tile, delay_e=delay_e, delay_i=delay_i, dt=dt)
+
+  def materialize(self, index_dtype=None):
+    """This just-in-time network with its connectivity stored: a CSR network with the same
+    neurons, weights, delays and state whose row j holds the postsynaptic neurons that the four
+    pull projections (outdim_parallel=True) connect presynaptic neuron j to, generated once
+    from the same streams (bp_jitconn_csr) instead of on every step.  Its steps are the
+    event-driven CSR products; with homogeneous weights both forms add exact event counts
+    times w, so the two networks spike alike, step for step.  The indices are int32 while
+    they fit (about 2e9 synapses), int64 beyond (or as `index_dtype` asks)."""
+    if self.jitconn is None:
+      raise ValueError("the network's connectivity is already stored")
+    if not bool(self.jitconn.get("outdim_parallel", True)):
+      raise ValueError("materialize takes the pull form (outdim_parallel=True); the push form runs on the "
+                       "whole-GPU runner")
+    L = _lib.lib()
+    dev, sp = self.device, _lib.stream_handle(self.device)
+    ne, n = self.n_exc, self.n
+    ni = n - ne
+    clen = _jitconn.conn_len(self.jitconn["prob"])
+    seeds = [_jitconn._seed(x, False) for x in self.jitconn["seeds"]]
+    # (outputs, inputs, seed, output offset): E2E, E2I from the excitatory rows, I2E, I2I from the
+    # inhibitory rows, as _propagate_ops calls them
+    projs = ((ne, ne, seeds[0], 0), (ni, ne, seeds[1], ne), (ne, ni, seeds[2], 0), (ni, ni, seeds[3], ne))
+    counts = []
+    for n_out, n_in, sd, _ in projs:
+      c = torch.zeros(max(n_in, 1), dtype=torch.int32, device=dev)
+      _lib.check(L.bp_jitconn_csr(0, clen, sd, n_out, n_in, _lib.ptr(c), None, 0, None, 0, _lib.BP_I32, sp),
+                 "jitconn_csr")
+      counts.append(c[:n_in].to(torch.int64))
+    row_len = torch.cat([counts[0] + counts[1], counts[2] + counts[3]])
+    indptr = torch.zeros(n + 1, dtype=torch.int64, device=dev)
+    torch.cumsum(row_len, 0, out=indptr[1:])
+    nnz = int(indptr[-1])
+    if index_dtype is None:
+      index_dtype = torch.int32 if nnz < 2 ** 31 - 1 else torch.int64
+    itype = _lib.BP_I32 if index_dtype == torch.int32 else _lib.BP_I64
+    indices = torch.empty(max(nnz, 1), dtype=index_dtype, device=dev)
+    bases = (indptr[:ne], indptr[:ne] + counts[0], indptr[ne:n], indptr[ne:n] + counts[2])
+    for (n_out, n_in, sd, off), base in zip(projs, bases):
+      base = base.contiguous()
+      _lib.check(L.bp_jitconn_csr(1, clen, sd, n_out, n_in, None, _lib.ptr(base), off, _lib.ptr(indices), nnz, itype,
+                                  sp), "jitconn_csr")
+    net = EINetwork(n, ne, indices=indices[:nnz], indptr=indptr.to(index_dtype), we=self.we, wi=self.wi,
+                    params=self.params, device=dev, V0=self.V, net_tile=self.net_tile, dt=self.delay_dt)
+    net.reset_state(self.V, self.ge, self.gi, self.t_last, self.spike, self.t_step)
+    # the same delays (in steps) and spike history
+    net.d_e, net.d_i, net.ring_len = self.d_e, self.d_i, self.ring_len
+    net.ring = self.ring.clone() if self.ring is not None else None
+    return net
 
   def reset_state(self, V, ge, gi, t_last, spike, t_step=0):
     """Overwrites the state (tensors of length n) and the time index."""
@@ -339,8 +390,11 @@ class EINetwork:
       n = self.n
       L = _lib.lib()
       ops = []
-      for (ind, ptr), m, w in zip(self._csr_split(), (self.n_exc, n - self.n_exc), (self.we, self.wi)):
-        wt = torch.full((1,), w, device=self.device)
+      # the weights as device scalars, kept for the network's life: an autotuned route is keyed
+      # by the arrays of the product, these included
+      if getattr(self, "_wts", None) is None:
+        self._wts = tuple(torch.full((1,), w, device=self.device) for w in (self.we, self.wi))
+      for (ind, ptr), m, wt in zip(self._csr_split(), (self.n_exc, n - self.n_exc), self._wts):
         out = torch.empty(n, device=self.device)
         plan = _event._plan_for(wt, ind, ptr, (m, n))
         ws, args = None, None
@@ -353,6 +407,24 @@ class EINetwork:
         ops.append((wt, out, plan, ws, args))
       self._opc = ops
     return self._opc
+
+  def tune_ops(self, spikes=None):
+    """Autotunes the per-operator path's two event products (event.autotune: row-parallel
+    kernel, the tiled plan's variants, the counting plan) on the rows' spikes of `spikes`
+    (default: the network's current spikes, so run it into its firing regime first).  Later
+    steps use the chosen kernels; every choice gives the same result bit for bit.  Returns
+    the two tuning records (excitatory rows, inhibitory rows)."""
+    if self.jitconn is not None:
+      raise ValueError("tune_ops tunes the CSR products of a network with stored connectivity")
+    sp = self.spike if spikes is None else spikes
+    ne, n = self.n_exc, self.n
+    self._csr_ops()
+    recs = [_event.autotune(wt, ind, ptr, ev, shape=(m, n))
+            for wt, (ind, ptr), m, ev in zip(self._wts, self._csr_split(), (ne, n - ne), (sp[:ne], sp[ne:]))]
+    self._opc = None  # rebuilt on the tuned routes
+    if hasattr(self, "_graph"):
+      del self._graph
+    return recs
 
   def _propagate_ops(self, T=None):
     """Conductance increments of one step (per-operator path): the rows' spikes of the

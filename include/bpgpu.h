@@ -178,6 +178,18 @@ bp_status bp_jitconn_mv(bp_jc_kind kind, bp_jc_vec vec_kind, const void* vec, in
 bp_status bp_jitconn_dense(bp_jc_kind kind, float p0, float p1, int32_t clen, uint32_t seed, int64_t num_row,
                            int64_t num_col, int32_t outdim_parallel, bp_jc_variant variant, float* dense,
                            bp_stream_t stream);
+/* The pull connectivity (Taichi GPU algorithm, outdim_parallel=1) of one projection with
+ * num_row outputs and num_col inputs, stored by input: for input column c, the output rows
+ * whose streams visit c.  Pass 0 writes counts[c] (num_col uint32: the column's rows).  Pass 1
+ * writes row + row_offset at indices[base[c] .. base[c] + counts[c]) (base: num_col int64,
+ * indices: BP_I32 or BP_I64, nnz entries; positions outside [0, nnz) are skipped), in no fixed
+ * order inside a column.  With the counts as row lengths this is the presynaptic-row CSR of the
+ * projection, the same connections the jitconn mv kernels generate on every call (replaces
+ * regenerating them: brainpy/_src/math/jitconn/_event_matvec_taichi.py:96-155 walks these
+ * streams per call). */
+bp_status bp_jitconn_csr(int32_t pass, int32_t clen, uint32_t seed, int64_t num_row, int64_t num_col,
+                         uint32_t* counts, const int64_t* base, int64_t row_offset, void* indices, int64_t nnz,
+                         bp_itype itype, bp_stream_t stream);
 
 /* ---------------------------------------------------------------------------
  * Column-tiled CSR plan (no counterpart in the reference; it plays the role of a

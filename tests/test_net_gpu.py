@@ -219,6 +219,46 @@ def test_jitconn_network_against_oracle(dyn, orc):
   assert rc.sum() > 300  # the network is active
 
 
+@pytest.mark.parametrize("index_dtype", [None, torch.int64])
+def test_materialized_jitconn_network(dyn, orc, index_dtype):
+  """EINetwork.materialize(): the four pull projections' connections stored as one
+  presynaptic-row CSR (bp_jitconn_csr) are the oracle's regeneration of the same streams, row
+  by row, and the stored network spikes as the just-in-time one does, bit for bit: its
+  per-operator path, the cluster runner and the whole-GPU runner against the just-in-time
+  network's per-operator path (exact event counts times w on every path)."""
+  ne, ni, prob, seeds = 1600, 400, 0.05, (11, 12, 13, 14)
+  n = ne + ni
+  V0 = _v0(n, seed=21)
+  a = dyn.EINetwork(n, ne, jitconn=dict(prob=prob, seeds=seeds), V0=V0)
+  m = a.materialize(index_dtype=index_dtype)
+  assert m.jitconn is None and m.indices.dtype == (index_dtype or torch.int32)
+  ep, ei, ip, ii = _jit_csr(orc, ne, ni, prob, seeds)
+  want_ptr = np.concatenate([ep.astype(np.int64), ip[1:].astype(np.int64) + int(ep[-1])])
+  want_ind = np.concatenate([ei, ii]).astype(np.int64)
+  ptr = m.indptr.cpu().numpy().astype(np.int64)
+  ind = m.indices.cpu().numpy().astype(np.int64)
+  np.testing.assert_array_equal(ptr, want_ptr)
+  rows = np.repeat(np.arange(n), np.diff(ptr))
+  got = np.lexsort((ind, rows))
+  want = np.lexsort((want_ind, rows))
+  np.testing.assert_array_equal(ind[got], want_ind[want])  # the same posts in every row
+  ca, _ = a.run(300, method="ops")
+  recs = m.tune_ops()  # the chosen kernels give the same products
+  assert len(recs) == 2 and all("choice" in r for r in recs)
+  runs = [m.run(300, method="ops")[0]]
+  for method in ("cluster", "grid"):
+    x = a.materialize(index_dtype=index_dtype)
+    x.reset_state(torch.as_tensor(V0, device="cuda"), torch.zeros(n, device="cuda"), torch.zeros(n, device="cuda"),
+                  torch.full((n,), -1e7, device="cuda"), torch.zeros(n, dtype=torch.bool, device="cuda"))
+    runs.append(x.run(300, method=method)[0])
+  for c in runs:
+    np.testing.assert_array_equal(c.cpu().numpy(), ca.cpu().numpy())
+  sa, sm = a.state_numpy(), m.state_numpy()
+  for k in ("V", "ge", "gi", "t_last", "spike"):
+    np.testing.assert_array_equal(sm[k], sa[k], err_msg=k)
+  assert int(ca.sum()) > 300  # the network is active
+
+
 def test_autotuned_tiles_and_concurrent_launches_match(dyn):
   """Networks of several size classes: tiles chosen by autotune_net_tiles and the launches of
   the cluster sizes run concurrently give the same spike counts and state, bit for bit, as

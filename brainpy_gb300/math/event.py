@@ -22,6 +22,24 @@ __all__ = ["csrmv", "csrmv_taichi", "csrmv_batch", "info", "CSRPlan", "prepare",
            "plan_cache_bytes"]
 
 
+def fix_point_params(bound):
+  """(k, tau) of a fixed-weight plan whose largest column sum of |w| is `bound`.  k is the
+  largest exponent with bound * 2^k <= 2^31 - 2^24: a column's integer weights q = rint(w * 2^k)
+  then add up below 2^31 in magnitude, the 2^24 covering the rounding of up to 2^25 entries a
+  column (0 <= k <= 100; k = 30 for an all-zero matrix).  A weight with |w| >= tau =
+  2^-(k+1) / 5e-6 is carried within 5e-6 of itself (|q * 2^-k - w| <= 2^-(k+1)); the nonzero
+  weights below tau go to the plan's float side list."""
+  k = 30 if bound <= 0.0 else int(math.floor(math.log2((2.0 ** 31 - 2.0 ** 24) / bound)))
+  k = max(0, min(k, 100))
+  return k, float(2.0 ** -(k + 1) / 5e-6)
+
+
+def fix_fits_24(wmax, k):
+  """Whether every integer weight rint(w * 2^k), |w| <= wmax, fits 24 bits (the 40-byte chunk
+  records): wmax * 2^k < 2^23 - 1 keeps the rounded magnitude below 2^23."""
+  return wmax * 2.0 ** k < 2.0 ** 23 - 1
+
+
 class CSRPlan:
   """Column-tiled layout of a CSR matrix for the event-driven (transpose) kernels.
 
@@ -91,9 +109,7 @@ class CSRPlan:
     colsum = torch.zeros(max(n, 1), dtype=torch.float64, device=dev)
     colsum.index_add_(0, indices.to(torch.int64), data.abs().to(torch.float64))
     bound = float(colsum.max()) if colsum.numel() else 0.0
-    k = 30 if bound <= 0.0 else int(math.floor(math.log2((2.0 ** 31 - 2.0 ** 24) / bound)))
-    k = max(0, min(k, 100))
-    tau = float(2.0 ** -(k + 1) / 5e-6)
+    k, tau = fix_point_params(bound)
     cnt = torch.zeros(1, dtype=torch.int64, device=dev)
     sp = _lib.stream_handle(dev)
     _lib.check(L.bp_csr_plan_fix_weights(ctypes.byref(self.c), k, tau, None, None, None, 0, _lib.ptr(cnt), 0, sp),
@@ -117,7 +133,7 @@ class CSRPlan:
     self.kind = "fixed"
     # the chunks as records (indices, integer weights): one read a segment
     wmax = float(data.abs().max()) if data.numel() else 0.0
-    rec = 40 if record != 48 and wmax * 2.0 ** k < 2.0 ** 23 - 1 else 48
+    rec = 40 if record != 48 and fix_fits_24(wmax, k) else 48
     if record == 40 and rec != 40:
       raise ValueError(f"40-byte records need max |w| * 2^k < 2^23 - 1 (max |w| = {wmax}, k = {k})")
     fxb = int(L.bp_csr_plan_fix_interleave_bytes(ctypes.byref(self.c), rec))

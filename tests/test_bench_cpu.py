@@ -32,3 +32,11 @@ def test_same_result_exact_and_tolerant():
   assert not bench.same_result(a, c, heter=True)
   z = torch.zeros(3)
   assert bench.same_result(z, z.clone(), heter=True)
+
+
+def test_profile_traffic_read_from_committed_summaries():
+  """The `traffic` key of the roofline comes from the committed ncu summaries: the headline
+  kernel's 53.0 MB a call and the weighted path's 123.0 MB (40-byte fixed-weight records)."""
+  assert bench.profile_traffic("event_csrmv_N1e6_K1000_rate2pct_homo.md") == 53_000_000
+  assert bench.profile_traffic("event_csrmv_N1e6_K1000_rate2pct_heter.md") == 123_000_000
+  assert bench.profile_traffic("no_such_summary.md") is None

@@ -432,14 +432,14 @@ def main():
     del data, ind, ptr, spikes, outs, g_run, g_warm, g_e2e, keep, singles
     event.release_plans()
     torch.cuda.empty_cache()
-    line["north_star_forms"] = north_star_forms(args)
+    line["forms"] = other_forms(args)
   if rank == 0:
     print(json.dumps(line))
   if ws > 1:
     torch.distributed.destroy_process_group()
 
 
-def north_star_forms(args):
+def other_forms(args):
   """The batched and served forms, the COBA example, the 4M-neuron jitconn network and a 1M-
   neuron CSR network on the whole-GPU runner, each timed with CUDA events under its own clock
   record, summarised beside the headline operator line."""

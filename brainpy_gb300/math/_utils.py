@@ -52,7 +52,7 @@ def float_data(data, device):
     t = t.reshape(1)
   if t.dtype != torch.float32:
     if t.dtype in (torch.float16, torch.bfloat16, torch.float64):
-      raise TypeError(f"only float32 data is supported by this build, got {t.dtype}")
+      raise TypeError(f"only float32 data is supported by this library, got {t.dtype}")
     raise TypeError(f"data must be a float array, got {t.dtype}")
   return t
 
@@ -72,5 +72,5 @@ def event_type(t, float_rule):
   if t.dtype == torch.float32:
     return float_rule, t
   if t.dtype in (torch.float16, torch.bfloat16, torch.float64):
-    raise TypeError(f"events of dtype {t.dtype} are not supported by this build (bool or float32)")
+    raise TypeError(f"events of dtype {t.dtype} are not supported by this library (bool or float32)")
   raise TypeError(f"events must be bool or float, got {t.dtype}")

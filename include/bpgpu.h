@@ -36,7 +36,7 @@ typedef enum {
   BP_ENOMEM = 4,   /* workspace / buffer too small */
   BP_ETIMEOUT = 5, /* a bounded device-side wait gave up */
   BP_ECUDA = 6,    /* CUDA runtime error */
-  BP_ENOTSUP = 7   /* valid request that this build does not implement */
+  BP_ENOTSUP = 7   /* valid request that this library does not implement */
 } bp_status;
 
 /* index type of CSR `indices` / `indptr` */

@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  This package restates the reference's algorithms on
 the CPU; it is imported by tests/, by __graft_entry__.smoke() and by the CPU
-baseline leg of bench.py, as the checker.  The brainpy_gb300 package never
+baseline leg of bench.py, to compare against.  The brainpy_gb300 package never
 imports it.
 """
 import ctypes

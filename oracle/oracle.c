@@ -1,7 +1,7 @@
 /*
  * oracle.c -- CPU restatement of BrainPy's event-driven synaptic propagation
  * path.  TEST INFRASTRUCTURE ONLY: the parity tests, the smoke check and the
- * CPU-baseline leg of bench.py use it as the checker; the product path never
+ * CPU-baseline leg of bench.py compare against it; the product path never
  * calls it.
  *
  * Compiled with -O2 -ffp-contract=off (no fast-math) so every float32

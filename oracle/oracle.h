@@ -1,6 +1,6 @@
 /*
  * oracle.h -- CPU restatement of BrainPy's event-driven synaptic propagation
- * path, used ONLY as test infrastructure (parity checker and the timed CPU
+ * path, used ONLY as test infrastructure (the parity reference and the timed CPU
  * baseline).  Nothing in the brainpy_gb300 package links or calls this code.
  *
  * Each function cites the reference file:line it restates (paths relative to
